@@ -1,0 +1,185 @@
+/*
+ * prrtc_gb300 — C ABI of a GB300-native (sm_103a) implementation of pRRTC's
+ * GPU RRT-Connect hot path.
+ *
+ * The reference exports only C++ templates:
+ *   - pRRTC::solve<Robot>(start, goals, env, settings)      src/planning/Planners.hh:75-78
+ *     (defined src/planning/pRRTC.cu:607-766, instantiated :768-771)
+ *   - ppln::collision::fkcc<Robot>(q, env, tid)              src/planning/utils.cuh:326-327
+ * This header is the C boundary that replaces both; include/prrtc/compat.hh
+ * rebuilds the reference's C++ signatures on top of it.
+ *
+ * Conventions
+ *   - Every array argument may be host memory or CUDA device memory of the
+ *     context's device; the library detects which (cudaPointerGetAttributes)
+ *     and copies host data itself.  Outputs follow the same rule.
+ *   - Configurations are row-major float32 [n][dof] in the reference's joint
+ *     order (Robots.hh).
+ *   - Calls on one context are serialised by an internal mutex; different
+ *     contexts are independent (no global device state, unlike the reference's
+ *     file-scope __device__ variables, pRRTC.cu:26-35).
+ *   - No call resets the device (the reference ends solve() with
+ *     cudaDeviceReset(), pRRTC.cu:764).
+ */
+#ifndef PRRTC_PRRTC_H
+#define PRRTC_PRRTC_H
+
+#include <stdint.h>
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum prrtc_status {
+    PRRTC_OK = 0,
+    PRRTC_EINVAL = 1,        /* bad argument (null, size, unknown robot, env too large) */
+    PRRTC_ENOMEM = 2,        /* device allocation failed, or a tree arena is full */
+    PRRTC_ETIMEDOUT = 3,     /* a device-side time budget ran out */
+    PRRTC_ECUDA = 4,         /* CUDA runtime error (see prrtc_last_error) */
+    PRRTC_EUNSUPPORTED = 5
+} prrtc_status;
+
+/* Robots of the reference (src/planning/Robots.hh:10-237). */
+typedef enum prrtc_robot {
+    PRRTC_ROBOT_SPHERE = 0,  /* toy 3-DoF point robot, radius 1 */
+    PRRTC_ROBOT_PANDA = 1,   /* 7-DoF */
+    PRRTC_ROBOT_FETCH = 2,   /* 8-DoF (q0 = prismatic torso) */
+    PRRTC_ROBOT_BAXTER = 3   /* 14-DoF, both arms */
+} prrtc_robot;
+
+typedef struct prrtc_ctx prrtc_ctx;
+typedef struct prrtc_env prrtc_env;
+
+/*
+ * Obstacles (replaces ppln::collision::Environment<float>,
+ * src/collision/environment.hh:11-44).  Flat float arrays in host memory;
+ * floats per obstacle:
+ *   spheres            4   x y z r                               (shapes.hh:271-290)
+ *   capsules           8   x1 y1 z1 xv yv zv r rdv               (shapes.hh:176-267)
+ *   z_aligned_capsules 8   same layout, axis along z
+ *   cylinders          8   accepted and ignored, like the reference checker,
+ *                          which never reads them (utils.cuh:211-242)
+ *   cuboids           15   x y z, axis_1 xyz, axis_2 xyz, axis_3 xyz,
+ *                          axis_1_r axis_2_r axis_3_r            (shapes.hh:75-171)
+ *   z_aligned_cuboids 15   same layout
+ * rdv is 1 / |(xv, yv, zv)|^2 as in the reference's factory.
+ */
+typedef struct prrtc_env_desc {
+    const float *spheres;
+    uint32_t num_spheres;
+    const float *capsules;
+    uint32_t num_capsules;
+    const float *z_aligned_capsules;
+    uint32_t num_z_aligned_capsules;
+    const float *cylinders;
+    uint32_t num_cylinders;
+    const float *cuboids;
+    uint32_t num_cuboids;
+    const float *z_aligned_cuboids;
+    uint32_t num_z_aligned_cuboids;
+} prrtc_env_desc;
+
+/* Largest environment one kernel stages in shared memory (obstacle floats
+ * after packing: 4 per sphere, 8 per capsule, 16 per cuboid). */
+#define PRRTC_MAX_ENV_FLOATS 12288
+
+/*
+ * Planner settings, byte-identical to pRRTC_settings
+ * (src/planning/pRRTC_settings.hh:3-16), same defaults via
+ * prrtc_settings_default().
+ */
+typedef struct prrtc_settings {
+    int max_samples;
+    int max_iters;
+    int num_new_configs;
+    int granularity;
+    float range;
+    int balance;
+    float tree_ratio;
+    bool dynamic_domain;
+    float dd_alpha;
+    float dd_radius;
+    float dd_min_radius;
+} prrtc_settings;
+
+/*
+ * Result of one query (replaces PlannerResult<Robot>, Planners.hh:11-23).
+ * The caller provides path storage: path_capacity rows of dof floats.  The
+ * path is written in the reference's order: goal first, then the goal-tree
+ * segment, the start-tree segment and the start (pRRTC.cu:731-741).
+ */
+typedef struct prrtc_result {
+    int solved;              /* 1 solved, 0 not */
+    int status;              /* prrtc_status of this query */
+    int start_tree_size;
+    int goal_tree_size;
+    int path_length;         /* nodes traced from both trees (pRRTC.cu:743) */
+    int iters;               /* iterations of the winning lane (-1 if unsolved) */
+    float cost;              /* sum of edge lengths traced (pRRTC.cu:561,571) */
+    int path_rows;           /* rows written to path */
+    int path_capacity;       /* in: rows available in path */
+    float *path;             /* in: [path_capacity][dof] host buffer, may be NULL */
+    uint64_t wall_ns;        /* whole call, host clock */
+    uint64_t kernel_ns;      /* planner kernel(s), device clock */
+    uint64_t copy_ns;        /* host<->device copies of the query */
+} prrtc_result;
+
+/* ---- context ------------------------------------------------------------ */
+prrtc_status prrtc_create(prrtc_ctx **out, int device);
+prrtc_status prrtc_destroy(prrtc_ctx *ctx);
+const char *prrtc_status_string(prrtc_status s);
+/* Text of the last error on this context (empty if none). */
+const char *prrtc_last_error(const prrtc_ctx *ctx);
+/* Total kernel launches this context has issued (for accounting). */
+uint64_t prrtc_launch_count(const prrtc_ctx *ctx);
+/* Planning margin: every robot sphere is inflated by pad metres while
+ * planning (default 0 = the reference's semantics).  A positive pad makes
+ * every returned path free under any checker whose sphere centres are within
+ * pad of this one's. */
+prrtc_status prrtc_set_planning_margin(prrtc_ctx *ctx, float pad);
+/* Device time budget of one planner launch in ns (0 = none, the default).
+ * When it runs out the query ends unsolved with status PRRTC_ETIMEDOUT. */
+prrtc_status prrtc_set_time_budget(prrtc_ctx *ctx, uint64_t ns);
+
+/* ---- robots ------------------------------------------------------------- */
+int prrtc_robot_dof(prrtc_robot robot);             /* -1 for an unknown robot */
+int prrtc_robot_num_spheres(prrtc_robot robot);     /* spheres of fk_spheres */
+/* Joint scaling of the reference sampler: q = u * scale + offset, u in [0,1)
+ * (Robots.hh scale_cfg).  Writes dof floats to each (host memory). */
+prrtc_status prrtc_robot_limits(prrtc_robot robot, float *scale, float *offset);
+
+/* ---- environments ------------------------------------------------------- */
+prrtc_status prrtc_env_upload(prrtc_ctx *ctx, const prrtc_env_desc *desc, prrtc_env **out);
+prrtc_status prrtc_env_free(prrtc_ctx *ctx, prrtc_env *env);
+
+/* ---- collision checking (replaces fkcc<Robot>, utils.cuh:326-33131) ----- */
+/* out_free[i] = 1 when configuration i is collision-free. */
+prrtc_status prrtc_validate_configs(prrtc_ctx *ctx, prrtc_robot robot, const prrtc_env *env,
+                                    const float *q, int64_t n, uint8_t *out_free);
+/*
+ * Edge i from a[i] to b[i] is free when every point
+ *     a + k * ((b - a) / granularity),  k = 1 .. granularity
+ * is free (the reference's extend interpolation, pRRTC.cu:430-442, evaluated
+ * in float32 without fused multiply-add).  granularity in [1, 1024].
+ */
+prrtc_status prrtc_validate_edges(prrtc_ctx *ctx, prrtc_robot robot, const prrtc_env *env,
+                                  const float *a, const float *b, int64_t n, int granularity,
+                                  uint8_t *out_free);
+/* World centre and radius of every model sphere: out is [n][num_spheres][4]. */
+prrtc_status prrtc_fk_spheres(prrtc_ctx *ctx, prrtc_robot robot, const float *q, int64_t n,
+                              float *out);
+
+/* ---- planning (replaces pRRTC::solve<Robot>, pRRTC.cu:607-766) ---------- */
+void prrtc_settings_default(prrtc_settings *s);
+/* goals: [num_goals][dof].  start/goals/path are host memory. */
+prrtc_status prrtc_solve(prrtc_ctx *ctx, prrtc_robot robot, const float *start, const float *goals,
+                         int num_goals, const prrtc_env *env, const prrtc_settings *settings,
+                         prrtc_result *result);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PRRTC_PRRTC_H */

@@ -1,0 +1,185 @@
+// Device-side building blocks shared by every robot's kernels: the packed
+// environment, the reference's sphere-vs-primitive tests, and the three
+// routines the generated checkers call for leaf spheres.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace prrtc {
+
+// 3x4 row-major rigid transform: r00 r01 r02 tx | r10 r11 r12 ty | r20 r21 r22 tz
+struct Frame {
+    float m[12];
+};
+
+// A self-collision leaf pair: sphere a in frame A, sphere b in frame B.
+struct LeafPair {
+    float4 a;
+    float4 b;
+};
+
+// Packed environment, float4 records, in this order (all 16-byte aligned):
+//   spheres  ns  x 1   (x, y, z, r)
+//   capsules nc  x 2   (x1, y1, z1, r) (xv, yv, zv, rdv)
+//   zcaps    nzc x 2   same
+//   cuboids  ncb x 4   (x, y, z, r1) (a1x, a1y, a1z, r2) (a2x, a2y, a2z, r3) (a3x, a3y, a3z, 0)
+//   zcuboids nzb x 4   same
+// The reference's cylinders array is never read by its checker and is not packed.
+struct EnvCounts {
+    int ns, nc, nzc, ncb, nzb;
+    __host__ __device__ int records() const { return ns + 2 * nc + 2 * nzc + 4 * ncb + 4 * nzb; }
+};
+
+struct EnvView {
+    const float4 *rec;   // records (shared memory once staged)
+    EnvCounts n;
+};
+
+// Copy a packed environment into shared memory (all threads of the block
+// participate; caller synchronises).
+__device__ __forceinline__ void stage_env(float4 *smem, const float4 *__restrict__ g, int records)
+{
+    for (int i = threadIdx.x; i < records; i += blockDim.x) smem[i] = __ldg(g + i);
+}
+
+// ---- the reference's primitive tests (src/planning/utils.cuh:58-209) ------
+// Each returns true when the sphere (x, y, z, r) intersects the primitive,
+// i.e. the reference's "< 0" on squared distance minus squared radius.
+
+__device__ __forceinline__ bool hit_sphere(float4 s, float x, float y, float z, float r)
+{
+    const float dx = x - s.x, dy = y - s.y, dz = z - s.z;
+    const float rs = r + s.w;
+    return dx * dx + dy * dy + dz * dz - rs * rs < 0.0f;
+}
+
+__device__ __forceinline__ bool hit_capsule(float4 a, float4 v, float x, float y, float z, float r)
+{
+    const float dot = (x - a.x) * v.x + (y - a.y) * v.y + (z - a.z) * v.z;
+    const float cdf = fmaxf(fminf(dot * v.w, 1.0f), 0.0f);
+    const float dx = x - (a.x + v.x * cdf), dy = y - (a.y + v.y * cdf), dz = z - (a.z + v.z * cdf);
+    const float rs = r + a.w;
+    return dx * dx + dy * dy + dz * dz - rs * rs < 0.0f;
+}
+
+__device__ __forceinline__ bool hit_z_capsule(float4 a, float4 v, float x, float y, float z, float r)
+{
+    const float dot = (z - a.z) * v.z;
+    const float cdf = fmaxf(fminf(dot * v.w, 1.0f), 0.0f);
+    const float dx = x - a.x, dy = y - a.y, dz = z - (a.z + v.z * cdf);
+    const float rs = r + a.w;
+    return dx * dx + dy * dy + dz * dz - rs * rs < 0.0f;
+}
+
+__device__ __forceinline__ bool hit_cuboid(float4 c0, float4 c1, float4 c2, float4 c3, float x, float y,
+                                           float z, float rsq)
+{
+    const float xs = x - c0.x, ys = y - c0.y, zs = z - c0.z;
+    const float a1 = fmaxf(0.0f, fabsf(c1.x * xs + c1.y * ys + c1.z * zs) - c0.w);
+    const float a2 = fmaxf(0.0f, fabsf(c2.x * xs + c2.y * ys + c2.z * zs) - c1.w);
+    const float a3 = fmaxf(0.0f, fabsf(c3.x * xs + c3.y * ys + c3.z * zs) - c2.w);
+    return a1 * a1 + a2 * a2 + a3 * a3 - rsq < 0.0f;
+}
+
+__device__ __forceinline__ bool hit_z_cuboid(float4 c0, float4 c1, float4 c2, float x, float y, float z,
+                                             float rsq)
+{
+    const float xs = x - c0.x, ys = y - c0.y, zs = z - c0.z;
+    const float a1 = fmaxf(0.0f, fabsf(c1.x * xs + c1.y * ys) - c0.w);
+    const float a2 = fmaxf(0.0f, fabsf(c2.x * xs + c2.y * ys) - c1.w);
+    const float a3 = fmaxf(0.0f, fabsf(zs) - c2.w);
+    return a1 * a1 + a2 * a2 + a3 * a3 - rsq < 0.0f;
+}
+
+// Sphere against every obstacle with early exit
+// (sphere_environment_in_collision, utils.cuh:211-242).  Not inlined: every
+// generated call site shares one copy of the obstacle loops.
+static __device__ __noinline__ bool env_hit(const EnvView e, float x, float y, float z, float r)
+{
+    const float4 *p = e.rec;
+    for (int i = 0; i < e.n.ns; i++)
+        if (hit_sphere(p[i], x, y, z, r)) return true;
+    p += e.n.ns;
+    for (int i = 0; i < e.n.nc; i++)
+        if (hit_capsule(p[2 * i], p[2 * i + 1], x, y, z, r)) return true;
+    p += 2 * e.n.nc;
+    for (int i = 0; i < e.n.nzc; i++)
+        if (hit_z_capsule(p[2 * i], p[2 * i + 1], x, y, z, r)) return true;
+    p += 2 * e.n.nzc;
+    const float rsq = r * r;
+    for (int i = 0; i < e.n.ncb; i++)
+        if (hit_cuboid(p[4 * i], p[4 * i + 1], p[4 * i + 2], p[4 * i + 3], x, y, z, rsq)) return true;
+    p += 4 * e.n.ncb;
+    for (int i = 0; i < e.n.nzb; i++)
+        if (hit_z_cuboid(p[4 * i], p[4 * i + 1], p[4 * i + 2], x, y, z, rsq)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void xform(const Frame &T, float4 c, float &x, float &y, float &z)
+{
+    x = T.m[0] * c.x + T.m[1] * c.y + T.m[2] * c.z + T.m[3];
+    y = T.m[4] * c.x + T.m[5] * c.y + T.m[6] * c.z + T.m[7];
+    z = T.m[8] * c.x + T.m[9] * c.y + T.m[10] * c.z + T.m[11];
+}
+
+// Leaf spheres (given in frame T) against the environment; true on first hit.
+// pad inflates every radius (0 reproduces the reference exactly).
+static __device__ __noinline__ bool env_leaves(const EnvView e, const Frame T, const float4 *__restrict__ leaves, int n,
+                                        float pad)
+{
+    for (int i = 0; i < n; i++) {
+        const float4 c = __ldg(leaves + i);
+        float x, y, z;
+        xform(T, c, x, y, z);
+        if (env_hit(e, x, y, z, c.w + pad)) return true;
+    }
+    return false;
+}
+
+// Leaf pairs: a in frame A, b in frame B, Tab = inv(T_A) * T_B; true when any
+// pair overlaps (sphere_sphere_self_collision, utils.cuh:83-86).  pad2 is the
+// added inflation of a pair (twice the per-sphere pad).
+static __device__ __noinline__ bool self_pairs(const Frame Tab, const LeafPair *__restrict__ pairs, int n, float pad2)
+{
+    for (int i = 0; i < n; i++) {
+        const float4 a = __ldg(&pairs[i].a);
+        const float4 b = __ldg(&pairs[i].b);
+        float x, y, z;
+        xform(Tab, b, x, y, z);
+        const float dx = a.x - x, dy = a.y - y, dz = a.z - z;
+        const float rs = a.w + b.w + pad2;
+        if (dx * dx + dy * dy + dz * dz - rs * rs < 0.0f) return true;
+    }
+    return false;
+}
+
+// What the generated checkers call.  pad = 0 and stop_flag = nullptr give the
+// reference checker's verdicts; planners may inflate every sphere by pad
+// (a certified margin) and share a block flag through which any lane's
+// collision ends the other lanes' work on the same edge.
+struct CheckCtx {
+    EnvView env;
+    float pad;
+    volatile int *stop_flag;
+    __device__ __forceinline__ bool env_hit(float x, float y, float z, float r) const
+    {
+        return prrtc::env_hit(env, x, y, z, r + pad);
+    }
+    __device__ __forceinline__ bool env_leaves(const Frame &T, const float4 *l, int n) const
+    {
+        return prrtc::env_leaves(env, T, l, n, pad);
+    }
+    __device__ __forceinline__ bool self_pairs(const Frame &T, const LeafPair *p, int n) const
+    {
+        return prrtc::self_pairs(T, p, n, 2.0f * pad);
+    }
+    __device__ __forceinline__ bool pair_hit(float dx, float dy, float dz, float rs) const
+    {
+        rs += 2.0f * pad;
+        return dx * dx + dy * dy + dz * dz - rs * rs < 0.0f;
+    }
+    __device__ __forceinline__ bool stop() const { return stop_flag != nullptr && *stop_flag != 0; }
+};
+
+}  // namespace prrtc

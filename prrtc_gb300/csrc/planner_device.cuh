@@ -1,0 +1,165 @@
+// Device pieces of the RRT-Connect planner shared by the plain (single-query,
+// drop-in) form and the batched form: Halton sampling, the nearest-neighbour
+// scan, dynamic-domain radius updates and path traceback.
+//
+// Trees are structure-of-arrays: coordinate d of node i of a tree lives at
+// nodes[d * cap + i] (cap a multiple of 4, so a thread reads four nodes per
+// 16-byte load).  Unwritten nodes hold NaN (the arena is filled with 0xFF
+// bytes), so a node whose coordinates are not all visible yet yields a NaN
+// distance, which never compares below the running minimum: the scan skips it
+// without the reference's explicit sentinel test (pRRTC.cu:297-303,390).
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+
+#include "device_common.cuh"
+#include "prrtc_internal.h"
+
+namespace prrtc {
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// One step of the reference's incremental Halton recurrence for dimension
+// count D (halton_next, pRRTC.cu:81-105), float32 exactly as written there.
+template <int D>
+__device__ __forceinline__ void halton_next(float *b, float *n, float *d, float *out)
+{
+#pragma unroll 1
+    for (int i = 0; i < D; i++) {
+        const float xf = d[i] - n[i];
+        if (xf == 1.0f) {
+            d[i] = floorf(d[i] * b[i]);
+            n[i] = 1.0f;
+        } else {
+            float y = floorf(d[i] / b[i]);
+            while (xf <= y) y = floorf(y / b[i]);
+            n[i] = floorf((b[i] + 1.0f) * y) - xf;
+        }
+        out[i] = n[i] / d[i];
+    }
+}
+
+// Block-wide nearest neighbour of s_q among the first `count` nodes of a tree.
+// Squared L2 accumulated as the reference does (sq_l2_dist, utils.cuh:100-109).
+// Ties resolve to the lowest node index.  Result in (s_out_d, s_out_i).
+template <int D>
+__device__ __forceinline__ void block_nn(const float *__restrict__ nodes, int cap, int count, const float *s_q,
+                                         float *s_red_d, int *s_red_i, float *s_out_d, int *s_out_i)
+{
+    float q[D];
+#pragma unroll
+    for (int d = 0; d < D; d++) q[d] = s_q[d];
+    float bd = FLT_MAX;
+    int bi = 0x7fffffff;
+    if (count > cap) count = cap;
+    const int n4 = (count + 3) >> 2;
+    const float4 *base = reinterpret_cast<const float4 *>(nodes);
+    const int cap4 = cap >> 2;
+    for (int c = threadIdx.x; c < n4; c += blockDim.x) {
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            const float4 v = __ldcg(base + (size_t)d * cap4 + c);
+            const float x0 = v.x - q[d], x1 = v.y - q[d], x2 = v.z - q[d], x3 = v.w - q[d];
+            a0 = fmaf(x0, x0, a0);
+            a1 = fmaf(x1, x1, a1);
+            a2 = fmaf(x2, x2, a2);
+            a3 = fmaf(x3, x3, a3);
+        }
+        const int i0 = 4 * c;
+        if (a0 < bd) { bd = a0; bi = i0; }
+        if (a1 < bd) { bd = a1; bi = i0 + 1; }
+        if (a2 < bd) { bd = a2; bi = i0 + 2; }
+        if (a3 < bd) { bd = a3; bi = i0 + 3; }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float od = __shfl_xor_sync(0xffffffffu, bd, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (od < bd || (od == bd && oi < bi)) { bd = od; bi = oi; }
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) {
+        s_red_d[warp] = bd;
+        s_red_i[warp] = bi;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        bd = lane < nw ? s_red_d[lane] : FLT_MAX;
+        bi = lane < nw ? s_red_i[lane] : 0x7fffffff;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const float od = __shfl_xor_sync(0xffffffffu, bd, off);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+            if (od < bd || (od == bd && oi < bi)) { bd = od; bi = oi; }
+        }
+        if (lane == 0) {
+            *s_out_d = bd;
+            *s_out_i = (bi == 0x7fffffff) ? 0 : bi;
+        }
+    }
+    __syncthreads();
+}
+
+// Dynamic-domain updates with the reference's CAS loops (pRRTC.cu:456-468,
+// 584-598), bounded so a contended radius cannot spin forever.
+__device__ __forceinline__ void dd_grow(float *r, float alpha)
+{
+    volatile float *rp = r;
+    for (int tries = 0; tries < 256; tries++) {
+        const float old = *rp;
+        if (old == FLT_MAX) return;
+        const float nw = old * (1.0f + alpha);
+        if (atomicCAS(reinterpret_cast<int *>(r), __float_as_int(old), __float_as_int(nw)) == __float_as_int(old)) return;
+    }
+}
+
+__device__ __forceinline__ void dd_shrink(float *r, float alpha, float radius0, float rmin)
+{
+    volatile float *rp = r;
+    for (int tries = 0; tries < 256; tries++) {
+        const float old = *rp;
+        const float nw = (old == FLT_MAX) ? radius0 : fmaxf(old * (1.0f - alpha), rmin);
+        if (atomicCAS(reinterpret_cast<int *>(r), __float_as_int(old), __float_as_int(nw)) == __float_as_int(old)) return;
+    }
+}
+
+// Walk parents from `start` to the root, recording node coordinates and adding
+// edge lengths (l2_dist, utils.cuh:89-98) to *cost.  Returns the number of
+// nodes recorded (root excluded) and the root in *root; -1 if out exceeds cap.
+template <int D>
+__device__ int trace_to_root(const float *nodes, const int *parents, int cap, int start, float *out, int out_cap,
+                             float *cost, int *root)
+{
+    int cur = start, n = 0;
+    const volatile int *vp = parents;
+    for (int steps = 0; steps <= cap; steps++) {
+        const int par = vp[cur];
+        if (par == cur) {
+            *root = cur;
+            return n;
+        }
+        if (n >= out_cap || par < 0 || par >= cap) return -1;
+        float acc = 0.0f;
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            const float a = __ldcg(nodes + (size_t)d * cap + cur);
+            const float b = __ldcg(nodes + (size_t)d * cap + par);
+            const float df = a - b;
+            acc = fmaf(df, df, acc);
+            out[n * D + d] = a;
+        }
+        *cost += sqrtf(acc);
+        n++;
+        cur = par;
+    }
+    return -1;
+}
+
+}  // namespace prrtc

@@ -1,0 +1,79 @@
+// Internal host-side declarations shared by the C ABI and the per-robot
+// kernel translation units.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "prrtc/prrtc.h"
+#include "device_common.cuh"
+
+namespace prrtc {
+
+// A packed environment as the kernels see it.
+struct LaunchEnv {
+    const float4 *rec;   // device records
+    EnvCounts counts;
+    int sms;             // SM count of the device
+};
+
+// Device control block of one query (replaces the reference's file-scope
+// __device__ globals solved, atomic_free_index, path_size, cost,
+// reached_goal_idx, solved_iters, pRRTC.cu:26-34).
+struct QueryCtl {
+    int solved;          // 0 running, 1 solved, -1 exhausted (iters or samples), -2 time budget
+    int free_index[2];   // next free node of each tree
+    int path_size[2];    // nodes traced from each tree
+    float cost;
+    int reached_goal;
+    int solved_iters;
+    int error;           // bit 0: path buffer too small
+    int pad_;
+};
+
+// Everything the plain-form planner kernel needs (passed by value).
+struct PlainParams {
+    // pRRTC_settings (pRRTC_settings.hh:3-16)
+    int max_samples, max_iters, num_new_configs, granularity;
+    float range;
+    int balance;
+    float tree_ratio;
+    int dynamic_domain;
+    float dd_alpha, dd_radius, dd_min_radius;
+    float pad;                         // collision margin added to every sphere (0 = reference)
+    unsigned long long budget_ns;      // device time budget (0 = none)
+    // two trees, nodes SoA: nodes[t][d * cap + i]
+    float *nodes[2];
+    int *parents[2];
+    float *radii[2];
+    int cap;
+    const float *halton_bases;         // [lanes][16] shuffled prime bases per lane
+    float scale[16], offset[16];       // joint scaling (Robots.hh scale_cfg)
+    const float4 *env;
+    EnvCounts env_n;
+    QueryCtl *ctl;
+    float *path;                       // [2][path_cap][dof]
+    int path_cap;
+};
+
+struct RobotOps {
+    int dof;
+    int num_spheres;
+    cudaError_t (*validate_configs)(const LaunchEnv &, const float *q, int64_t n, uint8_t *out, cudaStream_t);
+    cudaError_t (*validate_edges)(const LaunchEnv &, const float *a, const float *b, int64_t n, int g,
+                                  uint8_t *out, cudaStream_t);
+    cudaError_t (*fk_spheres)(const float *q, int64_t n, float *out, int sms, cudaStream_t);
+    cudaError_t (*solve_plain)(const PlainParams &, int threads, cudaStream_t);
+};
+
+// Shuffled Halton prime bases per sampling lane, as the reference seeds them
+// (pRRTC.cu:49-79,107-121): lane 0 keeps {3,5,...,59}; lane i > 0 shuffles
+// them with cuRAND XORWOW (seed 1 + i, subsequence i).
+cudaError_t launch_halton_bases(float *out, int lanes, cudaStream_t st);
+
+RobotOps robot_ops_sphere();
+RobotOps robot_ops_panda();
+RobotOps robot_ops_fetch();
+RobotOps robot_ops_baxter();
+
+}  // namespace prrtc

@@ -1,0 +1,414 @@
+"""Robot-model compiler: JSON collision models -> C tables + CUDA checkers.
+
+Input: ``prrtc_gb300/robots/<robot>.json`` (written by ``extract.py``).
+Output, for each robot:
+
+* ``csrc/robots/<robot>_model.h``: the model as plain-C tables
+  (``prrtc_joint_def`` ... from ``model_types.h``), read by the CPU oracle and
+  by host code;
+* ``csrc/robots/<robot>_fkcc.cuh``: a straight-line CUDA forward-kinematics
+  and collision-check routine for one configuration per thread.  Joint
+  transforms are folded at generation time (zero and unit entries of the
+  fixed transforms vanish), every frame lives in registers, and the checker
+  visits the model's groups in the reference's order.  The per-leaf work runs
+  in three small shared routines supplied by the caller (``Ctx``), so code
+  size stays proportional to the number of groups, not of sphere pairs:
+
+  - ``ctx.env_hit(x, y, z, r)``: sphere against every obstacle;
+  - ``ctx.env_leaves(T, leaves, n)``: leaf spheres given in frame T;
+  - ``ctx.self_pairs(Tab, pairs, n)``: sphere pairs (a in frame A, b in
+    frame B) given the relative transform Tab = inv(T_A) T_B;
+  - ``ctx.pair_hit(dx, dy, dz, ra + rb)``: gate pair overlap test;
+  - ``ctx.stop()``: cooperative early exit (another lane already failed).
+
+Usage: ``python -m prrtc_gb300.robots.codegen`` (no reference checkout needed).
+"""
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+CSRC = HERE.parent / "csrc" / "robots"
+ROBOTS = ("sphere", "panda", "fetch", "baxter")
+
+
+def load_model(robot: str) -> dict:
+    return json.loads((HERE / f"{robot}.json").read_text())
+
+
+def _lit(x: float) -> str:
+    x = float(x)
+    if x == int(x) and abs(x) < 1e6:
+        return f"{x:.1f}f"
+    return f"{x!r}f"
+
+
+# ------------------------------------------------------------------ C tables
+
+def emit_c_tables(m: dict) -> str:
+    R = m["robot"].capitalize()
+    out = []
+    w = out.append
+    w(f"// pRRTC {m['robot']} collision model as plain-C tables.  Generated by")
+    w("// prrtc_gb300/robots/codegen.py from the fitted model; do not edit.")
+    w(f"// Max |sphere centre - reference float64 FK|: {m['max_err']:.3e} m")
+    w("#pragma once")
+    w('#include "model_types.h"')
+    w("")
+    ne, ns = len(m["env_groups"]), len(m["self_groups"])
+    nl = sum(len(g["leaves"]) for g in m["env_groups"])
+    npairs = sum(len(g["pairs"]) for g in m["self_groups"])
+    w("enum {")
+    w(f"    k{R}Dof = {m['dof']},")
+    w(f"    k{R}NumJoints = {len(m['joints'])},")
+    w(f"    k{R}NumSpheres = {len(m['spheres'])},")
+    w(f"    k{R}NumEnvGroups = {ne},")
+    w(f"    k{R}NumEnvLeaves = {nl},")
+    w(f"    k{R}NumSelfGroups = {ns},")
+    w(f"    k{R}NumSelfPairs = {npairs},")
+    w(f"    k{R}NumSchedule = {len(m['schedule'])},")
+    w("};")
+    w("")
+    w(f"static const prrtc_joint_def k{R}Joints[] = {{")
+    for jt in m["joints"]:
+        F = [x for row in jt["F"] for x in row]
+        w("    {%d, %d, %d, {%s}}," % (jt["q"], jt["parent"], 1 if jt["type"] == "revolute" else 0,
+                                     ", ".join(_lit(x) for x in F)))
+    w("};")
+    w(f"static const prrtc_sphere_def k{R}Spheres[] = {{")
+    for s in m["spheres"]:
+        w("    {%d, %s, %s, %s, %s}," % (s["frame"], *[_lit(x) for x in s["c"]], _lit(s["r"])))
+    w("};")
+    w(f"static const prrtc_group_def k{R}EnvGroups[] = {{")
+    off = 0
+    for g in m["env_groups"]:
+        w("    {%d, -1, %d, %d},  /* %s */" % (g["gate"], off, len(g["leaves"]), g["label"]))
+        off += len(g["leaves"])
+    w("};")
+    allv = [x for g in m["env_groups"] for x in g["leaves"]]
+    w(f"static const short k{R}EnvLeaves[] = {{")
+    for i in range(0, len(allv), 16):
+        w("    " + ", ".join(str(x) for x in allv[i:i + 16]) + ",")
+    w("};")
+    if ns:
+        w(f"static const prrtc_group_def k{R}SelfGroups[] = {{")
+        off = 0
+        for g in m["self_groups"]:
+            w("    {%d, %d, %d, %d},  /* %s */" % (g["gate"][0], g["gate"][1], off, len(g["pairs"]), g["label"]))
+            off += len(g["pairs"])
+        w("};")
+        allp = [p for g in m["self_groups"] for p in g["pairs"]]
+        w(f"static const short k{R}SelfPairs[][2] = {{")
+        for i in range(0, len(allp), 8):
+            w("    " + " ".join("{%d, %d}," % tuple(p) for p in allp[i:i + 8]))
+        w("};")
+    else:
+        w(f"static const prrtc_group_def k{R}SelfGroups[] = {{{{-1, -1, 0, 0}}}};")
+        w(f"static const short k{R}SelfPairs[][2] = {{{{0, 0}}}};")
+    w(f"static const prrtc_sched_def k{R}Schedule[] = {{")
+    for i in range(0, len(m["schedule"]), 8):
+        w("    " + " ".join("{%d, %d}," % (0 if k == "env" else 1, g) for k, g in m["schedule"][i:i + 8]))
+    w("};")
+    w("")
+    return "\n".join(out)
+
+
+# ------------------------------------------------------- symbolic scalar code
+
+class _Code:
+    """Straight-line float code with constant folding of 0 / +-1 / literals."""
+
+    def __init__(self):
+        self.lines = []
+        self.n = 0
+
+    def tmp(self, expr, prefix="v"):
+        if isinstance(expr, float):
+            return expr
+        name = f"{prefix}{self.n}"
+        self.n += 1
+        self.lines.append(f"const float {name} = {expr};")
+        return name
+
+    @staticmethod
+    def term(coef: float, var):
+        """coef * var as (sign, text) or a folded constant."""
+        if isinstance(var, float):
+            return coef * var
+        if coef == 0.0:
+            return 0.0
+        if coef == 1.0:
+            return var
+        if coef == -1.0:
+            return f"(-{var})"
+        return f"{_lit(coef)} * {var}"
+
+    @staticmethod
+    def dot(pairs, const=0.0):
+        """sum(coef * var) + const; coef may be a float or a variable name,
+        var may be a variable name or a float."""
+        c = float(const)
+        terms = []
+        for a, b in pairs:
+            if isinstance(a, float) and isinstance(b, float):
+                c += a * b
+            elif isinstance(a, float) or isinstance(b, float):
+                k, v = (a, b) if isinstance(a, float) else (b, a)
+                if k == 0.0:
+                    continue
+                terms.append(_Code.term(k, v))
+            else:
+                terms.append(f"{a} * {b}")
+        if not terms:
+            return c
+        s = terms[0]
+        for t in terms[1:]:
+            if t.startswith("(-"):
+                s = f"{s} - {t[2:-1]}"
+            else:
+                s = f"{s} + {t}"
+        if c != 0.0:
+            s = f"{s} + {_lit(c)}" if c > 0 else f"{s} - {_lit(-c)}"
+        return s
+
+
+def _mat_of(F):
+    return [[float(F[i][k]) for k in range(4)] for i in range(3)]
+
+
+class _FkGen:
+    """Emits frame computations lazily, in chain order, into a _Code."""
+
+    def __init__(self, model, code: _Code):
+        self.m = model
+        self.code = code
+        self.frames = {-1: [[1.0, 0.0, 0.0, 0.0], [0.0, 1.0, 0.0, 0.0], [0.0, 0.0, 1.0, 0.0]]}
+        self.joint = {jt["q"]: jt for jt in model["joints"]}
+
+    def frame(self, j):
+        if j in self.frames:
+            return self.frames[j]
+        jt = self.joint[j]
+        P = self.frame(jt["parent"])
+        F = _mat_of(jt["F"])
+        c = self.code
+        # A = P * F   (3x4 affine composition)
+        A = [[None] * 4 for _ in range(3)]
+        for i in range(3):
+            for k in range(3):
+                A[i][k] = c.tmp(c.dot([(P[i][m], F[m][k]) for m in range(3)]), f"a{j}_")
+            A[i][3] = c.tmp(c.dot([(P[i][m], F[m][3]) for m in range(3)] + [(P[i][3], 1.0)]), f"a{j}_")
+        q = f"q[{j}]"
+        T = [[None] * 4 for _ in range(3)]
+        if jt["type"] == "revolute":
+            # T = A * Rz(q): columns 0 and 1 rotate, column 2 and the origin stay
+            s, co = f"s{j}", f"c{j}"
+            c.lines.append(f"float {s}, {co};")
+            c.lines.append(f"sincosf({q}, &{s}, &{co});")
+            for i in range(3):
+                T[i][0] = c.tmp(c.dot([(co, A[i][0]), (s, A[i][1])]), f"t{j}_")
+                T[i][1] = c.tmp(_sub(c, c.dot([(co, A[i][1])]), c.dot([(s, A[i][0])])), f"t{j}_")
+                T[i][2] = A[i][2]
+                T[i][3] = A[i][3]
+        else:
+            # T = A * Tz(q): the origin slides along column 2
+            for i in range(3):
+                T[i][0], T[i][1], T[i][2] = A[i][0], A[i][1], A[i][2]
+                T[i][3] = c.tmp(c.dot([(A[i][3], 1.0), (q, A[i][2])]), f"t{j}_")
+        self.frames[j] = T
+        return T
+
+    def point(self, f, xyz):
+        """World coordinates of a point given in frame f."""
+        T = self.frame(f)
+        return [self.code.tmp(self.code.dot([(T[i][k], float(xyz[k])) for k in range(3)] + [(T[i][3], 1.0)]), "p")
+                for i in range(3)]
+
+    def relative(self, fa, fb):
+        """Tab = inv(T_fa) * T_fb as a 3x4 of operands."""
+        c = self.code
+        Ta, Tb = self.frame(fa), self.frame(fb)
+        d = [c.tmp(_sub(c, Tb[i][3], Ta[i][3]), "d") for i in range(3)]
+        M = [[None] * 4 for _ in range(3)]
+        for i in range(3):
+            for k in range(3):
+                M[i][k] = c.tmp(c.dot([(Ta[m][i], Tb[m][k]) for m in range(3)]), "r")
+            M[i][3] = c.tmp(c.dot([(Ta[m][i], d[m]) for m in range(3)]), "r")
+        return M
+
+
+def _sub(c: _Code, a, b):
+    """a - b over operands/expressions (strings are wrapped)."""
+    if isinstance(a, float) and isinstance(b, float):
+        return a - b
+    if isinstance(b, float):
+        if b == 0.0:
+            return a
+        return f"({a}) - {_lit(b)}" if b > 0 else f"({a}) + {_lit(-b)}"
+    if isinstance(a, float) and a == 0.0:
+        return f"-({b})"
+    return f"({a}) - ({b})"
+
+
+def _frame_arg(M):
+    vals = []
+    for i in range(3):
+        for k in range(4):
+            v = M[i][k]
+            vals.append(_lit(v) if isinstance(v, float) else v)
+    return "Frame{{" + ", ".join(vals) + "}}"
+
+
+def emit_cuda_checker(m: dict) -> str:
+    name = m["robot"]
+    R = name.capitalize()
+    sp = m["spheres"]
+    code = _Code()
+    fk = _FkGen(m, code)
+    body = []
+
+    # leaf tables: env leaves grouped into same-frame blocks; self pairs into
+    # same-(frame a, frame b) blocks.  Blocks keep the reference's order.
+    leaf_rows, pair_rows = [], []
+    env_blocks, self_blocks = {}, {}
+    for gi, g in enumerate(m["env_groups"]):
+        blocks = []
+        for leaf in g["leaves"]:
+            f = sp[leaf]["frame"]
+            if not blocks or blocks[-1][0] != f:
+                blocks.append([f, len(leaf_rows), 0])
+            s = sp[leaf]
+            leaf_rows.append((s["c"][0], s["c"][1], s["c"][2], s["r"]))
+            blocks[-1][2] += 1
+        env_blocks[gi] = blocks
+    for gi, g in enumerate(m["self_groups"]):
+        blocks = []
+        for a, b in g["pairs"]:
+            fa, fb = sp[a]["frame"], sp[b]["frame"]
+            if not blocks or (blocks[-1][0], blocks[-1][1]) != (fa, fb):
+                blocks.append([fa, fb, len(pair_rows), 0])
+            pair_rows.append((sp[a]["c"], sp[a]["r"], sp[b]["c"], sp[b]["r"]))
+            blocks[-1][3] += 1
+        self_blocks[gi] = blocks
+
+    def env_block_calls(gi):
+        calls = []
+        for f, first, n in env_blocks[gi]:
+            T = fk.frame(f)
+            calls.append(f"ctx.env_leaves({_frame_arg(T)}, k{R}Leaf + {first}, {n})")
+        return calls
+
+    for kind, gi in m["schedule"]:
+        if kind == "env":
+            g = m["env_groups"][gi]
+            code.lines.append(f"// environment group {gi}: {g['label']}")
+            for f, _, _ in env_blocks[gi]:       # frames are shared: compute outside the if
+                fk.frame(f)
+            if g["gate"] >= 0:
+                s = sp[g["gate"]]
+                x, y, z = fk.point(s["frame"], s["c"])
+                code.lines.append(f"if (ctx.env_hit({_op(x)}, {_op(y)}, {_op(z)}, {_lit(s['r'])})) {{")
+                for call in env_block_calls(gi):
+                    code.lines.append(f"    if ({call}) return false;")
+                code.lines.append("}")
+            else:
+                for call in env_block_calls(gi):
+                    code.lines.append(f"if ({call}) return false;")
+        else:
+            g = m["self_groups"][gi]
+            code.lines.append(f"// self group {gi}: {g['label']}")
+            a, b = g["gate"]
+            sa, sb = sp[a], sp[b]
+            pa = fk.point(sa["frame"], sa["c"])
+            pb = fk.point(sb["frame"], sb["c"])
+            for fa, fb, _, _ in self_blocks[gi]:  # frames are shared: compute outside the if
+                fk.frame(fa)
+                fk.frame(fb)
+            dx, dy, dz = (code.tmp(_sub(code, pa[i], pb[i]), "g") for i in range(3))
+            code.lines.append(f"if (ctx.pair_hit({_op(dx)}, {_op(dy)}, {_op(dz)}, {_lit(sa['r'])} + {_lit(sb['r'])})) {{")
+            for fa, fb, first, n in self_blocks[gi]:
+                M = fk.relative(fa, fb)
+                code.lines.append(f"    if (ctx.self_pairs({_frame_arg(M)}, k{R}Pair + {first}, {n})) return false;")
+            code.lines.append("}")
+        code.lines.append("if (ctx.stop()) return true;")
+    code.lines.append("return true;")
+
+    # fk_spheres: every sphere's world centre (not on the validation hot path)
+    code2 = _Code()
+    fk2 = _FkGen(m, code2)
+    for i, s in enumerate(sp):
+        x, y, z = fk2.point(s["frame"], s["c"])
+        code2.lines.append(f"out[{i}] = make_float4({_op(x)}, {_op(y)}, {_op(z)}, {_lit(s['r'])});")
+
+    out = []
+    w = out.append
+    w(f"// Straight-line CUDA collision checker for pRRTC's {name} model.  Generated by")
+    w("// prrtc_gb300/robots/codegen.py from the fitted model; do not edit.")
+    w("// Semantics follow the reference checker fkcc<Robot> (src/planning/utils.cuh):")
+    w("// a leaf counts only when its group's gate (bounding sphere or bounding pair)")
+    w("// is hit; a config is free when no counted leaf is hit.")
+    w("#pragma once")
+    w("")
+    w(f"namespace prrtc {{ namespace gen_{name} {{")
+    w("")
+    w(f"constexpr int kDof = {m['dof']};")
+    w(f"constexpr int kNumSpheres = {len(sp)};")
+    w(f"constexpr int kNumLeaves = {max(1, len(leaf_rows))};")
+    w(f"constexpr int kNumPairs = {max(1, len(pair_rows))};")
+    w("")
+    w("// leaf spheres in their frame: (x, y, z, r)")
+    w(f"__device__ const float4 k{R}Leaf[kNumLeaves] = {{")
+    for r in leaf_rows or [(0.0, 0.0, 0.0, 0.0)]:
+        w("    {%s}," % ", ".join(_lit(v) for v in r))
+    w("};")
+    w("// sphere pairs: a = (x, y, z, r) in frame A, b = (x, y, z, r) in frame B")
+    w(f"__device__ const LeafPair k{R}Pair[kNumPairs] = {{")
+    for ca, ra, cb, rb in pair_rows or [([0, 0, 0], 0.0, [0, 0, 0], 0.0)]:
+        w("    {{%s, %s, %s, %s}, {%s, %s, %s, %s}}," % (*[_lit(v) for v in ca], _lit(ra), *[_lit(v) for v in cb], _lit(rb)))
+    w("};")
+    w("")
+    w("// Returns true when configuration q is collision-free.")
+    w("template <class Ctx>")
+    w("__device__ __forceinline__ bool fkcc(const float *__restrict__ q, Ctx &ctx)")
+    w("{")
+    for line in code.lines:
+        w("    " + line)
+    w("}")
+    w("")
+    w("// World centre and radius of every model sphere (model sphere order).")
+    w("__device__ __forceinline__ void fk_spheres(const float *__restrict__ q, float4 *__restrict__ out)")
+    w("{")
+    for line in code2.lines:
+        w("    " + line)
+    w("}")
+    w("")
+    w(f"}} }}  // namespace prrtc::gen_{name}")
+    w("")
+    return "\n".join(out)
+
+
+def _op(v):
+    return _lit(v) if isinstance(v, float) else v
+
+
+def write_all():
+    for r in ROBOTS:
+        m = load_model(r)
+        (CSRC / f"{r}_model.h").write_text(emit_c_tables(m))
+        (CSRC / f"{r}_fkcc.cuh").write_text(emit_cuda_checker(m))
+
+
+def check_up_to_date() -> list:
+    """Names of generated files that differ from what the JSON models give."""
+    stale = []
+    for r in ROBOTS:
+        m = load_model(r)
+        for path, text in ((CSRC / f"{r}_model.h", emit_c_tables(m)), (CSRC / f"{r}_fkcc.cuh", emit_cuda_checker(m))):
+            if not path.exists() or path.read_text() != text:
+                stale.append(path.name)
+    return stale
+
+
+if __name__ == "__main__":
+    write_all()
