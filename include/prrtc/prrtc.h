@@ -84,7 +84,7 @@ typedef struct prrtc_env_desc {
 
 /* Largest environment one kernel stages in shared memory (obstacle floats
  * after packing: 4 per sphere, 8 per capsule, 16 per cuboid). */
-#define PRRTC_MAX_ENV_FLOATS 12288
+#define PRRTC_MAX_ENV_FLOATS 11264
 
 /*
  * Planner settings, byte-identical to pRRTC_settings

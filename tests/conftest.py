@@ -1,0 +1,44 @@
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "oracle"))
+GOLDEN = ROOT / "tests" / "golden"
+REFERENCE = Path("/root/reference")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+def golden_cases():
+    return sorted(p.stem.replace("checker_", "") for p in GOLDEN.glob("checker_*.npz"))
+
+
+def load_golden(case: str):
+    from prrtc_gb300.env import Environment
+    z = np.load(GOLDEN / f"checker_{case}.npz")
+    env = Environment(spheres=z["env_spheres"], capsules=z["env_capsules"], z_aligned_capsules=z["env_z_capsules"],
+                      cuboids=z["env_cuboids"], z_aligned_cuboids=z["env_z_cuboids"])
+    return env, {k: z[k] for k in z.files}
+
+
+@pytest.fixture(scope="session")
+def oracle():
+    from pyoracle import OracleLib, build
+    build()
+    return OracleLib()
+
+
+@pytest.fixture(scope="session")
+def ctx():
+    import prrtc_gb300.build as b
+    b.build()
+    from prrtc_gb300 import Context
+    c = Context(0)
+    yield c
+    c.close()

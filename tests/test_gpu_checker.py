@@ -1,0 +1,95 @@
+"""GPU collision checker parity (validate_configs / validate_edges /
+fk_spheres through the C ABI) against the reference's verdicts and the oracle.
+
+Bar: every verdict equal, except configurations whose float64 near-contact
+measure (min |signed distance| over the checker's tests) is below 1e-5 m;
+those are counted and reported.  FK sphere centres within 1e-5 m of float64 FK.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden
+
+pytestmark = pytest.mark.gpu
+NEAR = 1e-5
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_checker_matches_reference_golden(case, ctx, oracle):
+    robot = case.split("_")[0]
+    env, z = load_golden(case)
+    got = ctx.validate_configs(robot, env, z["q"])
+    bad = np.flatnonzero(got != z["free_ref"])
+    print(f"{case}: {len(z['q'])} configs, mismatches {len(bad)}, near-contact {(z['margin'] < NEAR).sum()}")
+    assert np.all(z["margin"][bad] < NEAR)
+
+
+SCENES = [("panda", "tabletop", 0), ("panda", "shelf", 1), ("fetch", "mixed", 2), ("baxter", "shelf", 3)]
+
+
+@pytest.mark.parametrize("robot,kind,seed", SCENES)
+def test_checker_million_configs(robot, kind, seed, ctx, oracle):
+    from prrtc_gb300 import scenes
+    env = scenes.mixed_scene(seed, 60) if kind == "mixed" else (
+        scenes.shelf_scene(seed, 0.3 if robot == "baxter" else 0.0) if kind == "shelf" else scenes.tabletop_scene(seed))
+    sc, off = (np.array(v) for v in scenes.LIMITS[robot])
+    rng = np.random.default_rng(100 + seed)
+    q = (rng.random((1_000_000, len(sc))) * sc + off).astype(np.float32)
+    got = ctx.validate_configs(robot, env, q)
+    ref, margin = oracle.check(robot, env, q, margin=True)
+    bad = np.flatnonzero(got != ref)
+    near = int((margin < NEAR).sum())
+    print(f"{robot}/{kind}: 1e6 configs, free {ref.mean():.3f}, mismatches {len(bad)}, near-contact bucket {near}")
+    assert np.all(margin[bad] < NEAR)
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_fk_spheres_match_fp64(case, ctx, oracle):
+    robot = case.split("_")[0]
+    env, z = load_golden(case)
+    got = ctx.fk_spheres(robot, z["q"])
+    ref = oracle.fk_spheres(robot, z["q"].astype(np.float64))
+    assert np.abs(got[..., :3] - ref[..., :3]).max() < 1e-5
+    np.testing.assert_array_equal(got[..., 3], ref[..., 3].astype(np.float32))
+    # against the reference's own generated FK evaluated in float64
+    fk = ctx.fk_spheres(robot, z["fk_q"])
+    assert np.abs(fk[..., :3] - z["fk_centres"]).max() < 1e-5
+
+
+@pytest.mark.parametrize("robot,kind,seed", SCENES[:3])
+@pytest.mark.parametrize("g", [1, 32, 128])
+def test_edges_match_oracle(robot, kind, seed, g, ctx, oracle):
+    from prrtc_gb300 import scenes
+    env = scenes.mixed_scene(seed, 60) if kind == "mixed" else (
+        scenes.shelf_scene(seed) if kind == "shelf" else scenes.tabletop_scene(seed))
+    sc, off = (np.array(v) for v in scenes.LIMITS[robot])
+    rng = np.random.default_rng(7 + seed)
+    a = (rng.random((3000, len(sc))) * sc + off).astype(np.float32)
+    b = (a + rng.normal(0, 0.3, a.shape)).astype(np.float32)
+    got = ctx.validate_edges(robot, env, a, b, g)
+    ref = oracle.check_edges(robot, env, a, b, g)
+    bad = np.flatnonzero(got != ref)
+    for i in bad:   # a disagreement needs a near-contact point on that edge
+        step = (b[i] - a[i]) / np.float32(g)
+        pts = np.stack([a[i] + np.float32(k) * step for k in range(1, g + 1)]).astype(np.float32)
+        _, m = oracle.check(robot, env, pts, margin=True)
+        assert m.min() < NEAR
+    print(f"{robot} g={g}: {len(a)} edges, free {ref.mean():.3f}, mismatches {len(bad)}")
+
+
+def test_device_pointers_and_edge_cases(ctx, oracle):
+    import torch
+    from prrtc_gb300 import PrrtcError, scenes
+    from prrtc_gb300.env import Environment
+    env, z = load_golden("panda_tabletop")
+    q = z["q"]
+    host = ctx.validate_configs("panda", env, q)
+    dev = ctx.validate_configs("panda", env, torch.from_numpy(q).cuda()).cpu().numpy()
+    np.testing.assert_array_equal(host, dev)
+    assert len(ctx.validate_configs("panda", env, np.zeros((0, 7), np.float32))) == 0
+    empty = Environment()
+    free = ctx.validate_configs("panda", empty, q)
+    np.testing.assert_array_equal(free, oracle.check("panda", empty, q))
+    big = Environment(cuboids=np.zeros((800, 15), np.float32))
+    with pytest.raises(PrrtcError):
+        ctx.upload_env(big)
