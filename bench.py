@@ -1,0 +1,327 @@
+"""Benchmark: batched GPU RRT-Connect (solved queries/s) on 1024 Panda queries.
+
+One step = solving one batch of queries (default: 1024 seeded Panda
+narrow-passage shelf queries with the reference's shelf settings:
+granularity 128, balance 2, tree_ratio 1, dynamic domain on).  Prints one
+JSON line (the contract this repository's driver reads):
+
+  value      solved queries/s of the batched persistent kernel, inputs resident
+             in HBM, timed with CUDA events on the launching stream, L2
+             flushed between steps
+  e2e        the same through prrtc_solve_batch with host buffers (upload,
+             solve, download inside the timed region)
+  plain      the drop-in single-query form (prrtc_solve) on a sample of the
+             same queries, one at a time
+  roofline   the planner kernel's algorithmic FP32 FLOPs (counted in-kernel:
+             canonical FK + the reference checker's executed tests x weights)
+             per launch / launch time, against the device's measured FP32 FMA
+             peak (neither the HBM nor the tensor roof applies: the validator
+             is SIMT FP32 work on L1/L2-resident data)
+  cpu_baseline  the CPU restatement of pRRTC's algorithm (oracle, all host
+             threads) on a bounded sample of the same queries
+
+`--impl reference` times that CPU restatement alone (the reference has no
+other runnable implementation on this machine).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD_SETTINGS = {
+    # configs[1]: Panda shelf, granularity 128, balance 2, tree_ratio 1, DD (4, 1e-4, 1); other fields default
+    "panda_shelf": dict(granularity=128, balance=2, tree_ratio=1.0, dynamic_domain=True, dd_radius=4.0,
+                        dd_alpha=1e-4, dd_min_radius=1.0),
+    # configs[0]: Panda tabletop, range 1.0, granularity 32, 256 lanes, 100k samples, balance 0, DD off
+    "panda_tabletop": dict(max_samples=100000, num_new_configs=256, granularity=32, range=1.0, balance=0,
+                           dynamic_domain=False),
+    "fetch_mixed": dict(granularity=64),
+    "baxter_mixed": dict(granularity=128, balance=1, tree_ratio=0.5),
+}
+MARGIN = 1e-5   # planning margin (m): every returned path clears contact by 10 micrometres
+GPU_BUDGET_NS = int(30e9)   # per batch launch; unsolved queries past it count as failures
+CPU_BUDGET_S = 20.0         # per query in the CPU restatement
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device, self.rows, self.proc = device, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self) -> dict:
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": float(self.rows[0][1]) if self.rows[0][1].replace(".", "").isdigit() else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def settings_for(name):
+    from prrtc_gb300 import Settings
+    return Settings(**WORKLOAD_SETTINGS[name])
+
+
+def oracle_lib():
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from pyoracle import OracleLib, build
+    build()
+    return OracleLib()
+
+
+def cpu_planner(robot, qs, settings, threads):
+    """pRRTC's algorithm restated on the CPU (oracle), OpenMP over queries."""
+    O = oracle_lib()
+    t = time.perf_counter()
+    res, _ = O.solve_many(robot, np.stack([q.start for q in qs]), np.stack([q.goal for q in qs]),
+                          [q.env for q in qs], settings, threads=threads, path_cap=16, budget_s=CPU_BUDGET_S)
+    dt = time.perf_counter() - t
+    return sum(r.solved for r in res), dt, res
+
+
+def cpu_sample_size(name):
+    return {"panda_tabletop": 256, "panda_shelf": 64, "fetch_mixed": 64, "baxter_mixed": 32}[name]
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    from prrtc_gb300 import workloads
+    robot = workloads.WORKLOADS[args.workload][0]
+    qs = workloads.make(args.workload, args.queries)
+    ns = min(cpu_sample_size(args.workload), len(qs))
+    threads = os.cpu_count() or 1
+    s = settings_for(args.workload)
+    for _ in range(args.warmup):
+        cpu_planner(robot, qs[:max(1, ns // 8)], s, threads)
+    tot_solved, tot_dt = 0, 0.0
+    for k in range(args.steps):
+        sample = qs[(k * ns) % len(qs):][:ns]
+        solved, dt, _ = cpu_planner(robot, sample, s, threads)
+        tot_solved += solved
+        tot_dt += dt
+    v = tot_solved / tot_dt
+    line = {"impl": "reference", "metric": metric_name(args), "value": v, "unit": "queries/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_of(args),
+            "cpu_baseline": {"value": v, "unit": "queries/s", "cores": threads, "kind": "port",
+                             "sample": f"{ns} of the {len(qs)} queries per step"},
+            "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def metric_name(args):
+    return f"solved queries/s, batched, {args.queries} {args.workload} queries (1 GB300, 100% revalidated)"
+
+
+def config_of(args):
+    return {"workload": f"{args.workload}_{args.queries}", "queries": args.queries,
+            "settings": WORKLOAD_SETTINGS[args.workload], "planning_margin_m": MARGIN,
+            "l2": "flushed between steps (256 MiB write)", "parallelism": "queries sharded over ranks"}
+
+
+def h2d_bytes(qs):
+    b = 0
+    for q in qs:
+        e = q.env
+        b += 4 * (4 * len(e.spheres) + 8 * (len(e.capsules) + len(e.z_aligned_capsules)) +
+                  16 * (len(e.cuboids) + len(e.z_aligned_cuboids)))
+        b += 4 * (len(q.start) + len(q.goal)) + 24
+    return b
+
+
+def ours(args, rank, world):
+    import torch
+    from prrtc_gb300 import BatchSettings, Context, build, workloads
+    build.build()
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    robot = workloads.WORKLOADS[args.workload][0]
+    qs = workloads.make(args.workload, args.queries, seed0=rank * args.queries)
+    plan = settings_for(args.workload)
+    ctx = Context(dev)
+    envs = [ctx.upload_env(q.env) for q in qs]
+    bs = BatchSettings(plan, use_graph=1, margin=MARGIN, time_budget_ns=GPU_BUDGET_NS)
+    batch = ctx.batch(robot, [(e, q.start, q.goal) for e, q in zip(envs, qs)], bs, path_capacity=2048)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=f"cuda:{dev}")
+    launches0 = ctx.launches
+    for _ in range(args.warmup):
+        batch.run()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    kernel_ns, solved, flops, cfgs, nn_nodes, results = 0, 0, 0, 0, 0, None
+    launches0 = ctx.launches
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            batch.run()
+            st = batch.stats()
+            kernel_ns += st["kernel_ns"]
+            flops += st["flops"]
+            cfgs += st["configs_checked"]
+            nn_nodes += st["nn_nodes"]
+            results = batch.results()
+            solved += sum(r.solved for r in results)
+    torch.cuda.synchronize()
+    launches = ctx.launches - launches0
+    t_dev = kernel_ns * 1e-9
+    if world > 1:
+        t = torch.tensor([t_dev], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(t.item())
+        c = torch.tensor([float(solved)], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(c)
+        solved = int(c.item())
+    value = solved / t_dev
+    lat = [r.kernel_ns / 1e6 for r in results if r.solved]
+
+    # ---- e2e through the C ABI with host buffers
+    e2e_solved, e2e_t = 0, 0.0
+    host_q = [(q.env, q.start, q.goal) for q in qs]
+    ctx.solve_batch(robot, host_q[:64], bs)
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = ctx.solve_batch(robot, host_q, bs, path_capacity=2048)
+        e2e_t += time.perf_counter() - t0
+        e2e_solved += sum(r.solved for r in res)
+    d2h = sum(len(r.path) * r.path.shape[1] * 4 for r in res) + 64 * len(res)
+
+    if rank != 0:
+        return
+    # ---- revalidation of every returned path (last timed step) by the oracle checker
+    O = oracle_lib()
+    g = plan.granularity
+    bad = 0
+    for q, r in zip(qs, results):
+        if r.solved and not O.check_edges(robot, q.env, r.path[:-1], r.path[1:], g).all():
+            bad += 1
+    n_solved_last = sum(r.solved for r in results)
+
+    # ---- the plain single-query form on a sample
+    ns_plain = min(64, len(qs))
+    plain_t, plain_solved, plain_ms = 0.0, 0, []
+    ctx.set_planning_margin(MARGIN)
+    for q, e in zip(qs[:ns_plain], envs[:ns_plain]):
+        r = ctx.solve(robot, q.start, q.goal, e, plan)
+        plain_t += r.wall_ns * 1e-9
+        plain_solved += r.solved
+        plain_ms.append(r.wall_ns / 1e6)
+    plain_qps = plain_solved / plain_t
+
+    # ---- roofline: FP32 work of the planner kernel vs the measured FP32 peak
+    peak = ctx.measure_fp32_peak()
+    achieved = flops / t_dev / 1e12
+    nn_bytes = nn_nodes * 4 * plan_dof(robot)
+
+    # ---- CPU baseline (bounded sample)
+    ns_cpu = min(cpu_sample_size(args.workload), len(qs))
+    threads = os.cpu_count() or 1
+    cs, cdt, _ = cpu_planner(robot, qs[:ns_cpu], plan, threads)
+
+    line = {
+        "metric": metric_name(args), "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_of(args),
+        "p50_solve_ms": statistics.median(lat) if lat else None,
+        "p99_solve_ms": float(np.percentile(lat, 99)) if lat else None,
+        "success_rate": n_solved_last / len(qs), "revalidated": f"{n_solved_last - bad}/{n_solved_last}",
+        "edge_validations_per_s": cfgs / plan.granularity / t_dev,
+        "configs_per_s": cfgs / t_dev,
+        "plain": {"queries_per_s": plain_qps, "p50_solve_ms": statistics.median(plain_ms), "sample": ns_plain,
+                  "batched_over_plain": value / plain_qps},
+        "e2e": {"value": e2e_solved / e2e_t, "unit": "queries/s", "h2d_bytes_per_step": h2d_bytes(qs),
+                "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": "measured FP32 FMA chain kernel on this GPU (prrtc_measure_fp32_peak)",
+                     "nn_scan_bytes_per_s": nn_bytes / t_dev},
+        "cpu_baseline": {"value": cs / cdt, "unit": "queries/s", "cores": threads, "kind": "port",
+                         "sample": f"first {ns_cpu} of the {len(qs)} queries, oracle RRT-Connect restatement"},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def plan_dof(robot):
+    return {"sphere": 3, "panda": 7, "fetch": 8, "baxter": 14}[robot]
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="panda_shelf", choices=sorted(WORKLOAD_SETTINGS))
+    ap.add_argument("--queries", type=int, default=1024)
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.warmup < 3:
+        log("warmup raised to 3")
+        args.warmup = 3
+    if world > 1:
+        import torch
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        if backend == "nccl":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        torch.distributed.init_process_group(backend)
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+    else:
+        ours(args, rank, world)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -172,12 +172,78 @@ prrtc_status prrtc_validate_edges(prrtc_ctx *ctx, prrtc_robot robot, const prrtc
 prrtc_status prrtc_fk_spheres(prrtc_ctx *ctx, prrtc_robot robot, const float *q, int64_t n,
                               float *out);
 
+/* Work counters: algorithmic FLOPs (weights as prrtc_batch_stats.flops) and
+ * configurations checked by validate_configs / validate_edges / solve since
+ * the last reset. */
+prrtc_status prrtc_work_counters(prrtc_ctx *ctx, uint64_t *flops, uint64_t *configs, int reset);
+/* Diagnostic: FP32 FMA throughput of the device in TFLOP/s, measured with a
+ * chain-of-FMA kernel over every SM (the roofline denominator of the
+ * validator, which runs on the FP32 pipe). */
+prrtc_status prrtc_measure_fp32_peak(prrtc_ctx *ctx, double *tflops);
+
 /* ---- planning (replaces pRRTC::solve<Robot>, pRRTC.cu:607-766) ---------- */
 void prrtc_settings_default(prrtc_settings *s);
 /* goals: [num_goals][dof].  start/goals/path are host memory. */
 prrtc_status prrtc_solve(prrtc_ctx *ctx, prrtc_robot robot, const float *start, const float *goals,
                          int num_goals, const prrtc_env *env, const prrtc_settings *settings,
                          prrtc_result *result);
+
+/* ---- batched planning (no reference counterpart: pRRTC solves one query per
+ * call; its only callers loop over problems, scripts/evaluate_mbm.cpp:126-151) */
+
+/* One query of a batch.  The environment is either an uploaded prrtc_env or
+ * host arrays (env = NULL), which the batch packs and uploads itself. */
+typedef struct prrtc_query {
+    const prrtc_env *env;
+    const prrtc_env_desc *env_desc;
+    const float *start;              /* [dof], host */
+    const float *goals;              /* [num_goals][dof], host */
+    int num_goals;
+} prrtc_query;
+
+typedef struct prrtc_batch_settings {
+    prrtc_settings plan;             /* applied to every query; num_new_configs = virtual sampling lanes */
+    int max_nodes_per_tree;          /* arena capacity per tree (0: min(max_samples, 16384)) */
+    int max_active;                  /* resident query slots (0: all queries, within the arena budget) */
+    int warps_per_block;             /* 0: 4 */
+    int blocks_per_sm;               /* 0: occupancy maximum */
+    int use_graph;                   /* replay each run as a captured CUDA graph */
+    float margin;                    /* sphere inflation while planning, metres (>= 0) */
+    uint64_t time_budget_ns;         /* 0: none */
+} prrtc_batch_settings;
+
+typedef struct prrtc_batch prrtc_batch;
+
+/* Totals of the last run of a batch. */
+typedef struct prrtc_batch_stats {
+    uint64_t kernel_ns;              /* planner launch, device clock */
+    int64_t samples;                 /* samples drawn over all queries */
+    int solved;                      /* queries solved */
+    int blocks, warps_per_block;     /* launch shape used */
+    int slots;                       /* resident query slots */
+    int error;                       /* nonzero: a worker gave up waiting for work */
+    uint64_t configs_checked;        /* configurations validated (edge points examined) */
+    uint64_t flops;                  /* algorithmic FLOPs of those checks: forward kinematics
+                                        2 (12 dof + 9 spheres) per config, plus the primitive
+                                        tests executed x {sphere 11, capsule 26, z-capsule 16,
+                                        cuboid 27, z-cuboid 18, sphere pair 11} */
+    uint64_t nn_nodes;               /* tree nodes visited by nearest-neighbour scans */
+} prrtc_batch_stats;
+
+void prrtc_batch_settings_default(prrtc_batch_settings *s);
+/* Packs and uploads the queries and allocates the batch's device state. */
+prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, const prrtc_query *queries, int n,
+                                const prrtc_batch_settings *settings, prrtc_batch **out);
+/* Solves every query of the batch in one persistent launch; inputs and
+ * results stay on the device.  A batch may be run again (same answers). */
+prrtc_status prrtc_batch_run(prrtc_ctx *ctx, prrtc_batch *batch);
+/* Copies the last run's results (and paths into each result's buffer). */
+prrtc_status prrtc_batch_results(prrtc_ctx *ctx, prrtc_batch *batch, prrtc_result *results);
+prrtc_status prrtc_batch_stats_get(prrtc_ctx *ctx, const prrtc_batch *batch, prrtc_batch_stats *stats);
+prrtc_status prrtc_batch_free(prrtc_ctx *ctx, prrtc_batch *batch);
+/* create + run + results + free. */
+prrtc_status prrtc_solve_batch(prrtc_ctx *ctx, prrtc_robot robot, const prrtc_query *queries, int n,
+                               const prrtc_batch_settings *settings, prrtc_result *results);
 
 #ifdef __cplusplus
 }

@@ -14,6 +14,7 @@
 
 #include <float.h>
 #include <math.h>
+#include <time.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -487,6 +488,13 @@ static int tree_push(tree_t *t, int dof)
     return t->count++;
 }
 
+static double now_s(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
 static uint64_t splitmix64(uint64_t *s)
 {
     uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
@@ -613,7 +621,12 @@ int oracle_solve(int robot, const float *start, const float *goals, int num_goal
     }
     int solved = 0, win_iter = -1, junction_t = -1, junction_o = -1, win_t = 0;
     const float fg = (float)g;
+    const double deadline = S->budget_s > 0 ? now_s() + S->budget_s : 0;
     while (!solved) {
+        if (deadline > 0 && now_s() > deadline) {
+            solved = -2;
+            break;
+        }
         for (int bid = 0; bid < L && !solved; bid++) {
             int iter = ++iters[bid];
             if (iter > S->max_iters) {

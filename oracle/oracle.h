@@ -69,6 +69,7 @@ typedef struct oracle_settings {
     float tree_ratio;
     int dynamic_domain;
     float dd_alpha, dd_radius, dd_min_radius;
+    double budget_s;         /* wall-clock budget per query, 0 = none (then unsolved) */
 } oracle_settings;
 
 typedef struct oracle_result {

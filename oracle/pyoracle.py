@@ -27,7 +27,7 @@ class OSettings(C.Structure):
     _fields_ = [("max_samples", C.c_int), ("max_iters", C.c_int), ("num_new_configs", C.c_int),
                 ("granularity", C.c_int), ("range", C.c_float), ("balance", C.c_int), ("tree_ratio", C.c_float),
                 ("dynamic_domain", C.c_int), ("dd_alpha", C.c_float), ("dd_radius", C.c_float),
-                ("dd_min_radius", C.c_float)]
+                ("dd_min_radius", C.c_float), ("budget_s", C.c_double)]
 
 
 class OResult(C.Structure):
@@ -116,8 +116,9 @@ class OracleLib:
         return out
 
     @staticmethod
-    def settings(s) -> OSettings:
-        d = s if isinstance(s, dict) else s.as_dict()
+    def settings(s, budget_s: float = 0.0) -> OSettings:
+        d = dict(s if isinstance(s, dict) else s.as_dict())
+        d.setdefault("budget_s", budget_s)
         o = OSettings()
         for k, _ in OSettings._fields_:
             setattr(o, k, int(d[k]) if k == "dynamic_domain" else d[k])
@@ -137,7 +138,7 @@ class OracleLib:
         assert rc == 0
         return r, path[:r.path_rows].copy() if r.solved else None
 
-    def solve_many(self, robot, starts, goals, envs, settings, threads=0, path_cap=4096):
+    def solve_many(self, robot, starts, goals, envs, settings, threads=0, path_cap=4096, budget_s=0.0):
         D = self.dof(robot)
         starts, goals = _arr(starts, D), _arr(goals, D)
         refs = [_EnvRef(e) for e in envs]
@@ -145,7 +146,7 @@ class OracleLib:
         res = (OResult * len(refs))()
         paths = np.empty((len(refs), path_cap, D), np.float32)
         rc = self.L.oracle_solve_many(ROBOTS[robot], len(refs), starts.ctypes.data, goals.ctypes.data, earr,
-                                      C.byref(self.settings(settings)), paths.ctypes.data, path_cap, res, threads)
+                                      C.byref(self.settings(settings, budget_s)), paths.ctypes.data, path_cap, res, threads)
         assert rc == 0
         return list(res), paths
 

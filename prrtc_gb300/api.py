@@ -70,6 +70,32 @@ class _Result(C.Structure):
                 ("kernel_ns", C.c_uint64), ("copy_ns", C.c_uint64)]
 
 
+class _Query(C.Structure):
+    _fields_ = [("env", C.c_void_p), ("env_desc", C.c_void_p), ("start", C.c_void_p), ("goals", C.c_void_p),
+                ("num_goals", C.c_int)]
+
+
+class BatchSettings(C.Structure):
+    """prrtc_batch_settings: planner settings for every query plus the batch's
+    arena, launch shape, CUDA-graph and margin options."""
+    _fields_ = [("plan", Settings), ("max_nodes_per_tree", C.c_int), ("max_active", C.c_int),
+                ("warps_per_block", C.c_int), ("blocks_per_sm", C.c_int), ("use_graph", C.c_int),
+                ("margin", C.c_float), ("time_budget_ns", C.c_uint64)]
+
+    def __init__(self, plan: Settings | None = None, **kw):
+        super().__init__()
+        self.plan = plan if plan is not None else Settings()
+        self.time_budget_ns = int(60e9)     # a guard for interactive use; 0 = unbounded (the C default)
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+
+class _BatchStats(C.Structure):
+    _fields_ = [("kernel_ns", C.c_uint64), ("samples", C.c_int64), ("solved", C.c_int), ("blocks", C.c_int),
+                ("warps_per_block", C.c_int), ("slots", C.c_int), ("error", C.c_int),
+                ("configs_checked", C.c_uint64), ("flops", C.c_uint64), ("nn_nodes", C.c_uint64)]
+
+
 @dataclass
 class PlannerResult:
     """Mirror of PlannerResult<Robot> (Planners.hh:11-23); path is goal first."""
@@ -111,6 +137,15 @@ def lib():
             "prrtc_fk_spheres": (C.c_int, [vp, C.c_int, fp, i64, fp]),
             "prrtc_settings_default": (None, [C.POINTER(Settings)]),
             "prrtc_solve": (C.c_int, [vp, C.c_int, fp, fp, C.c_int, vp, C.POINTER(Settings), C.POINTER(_Result)]),
+            "prrtc_measure_fp32_peak": (C.c_int, [vp, C.POINTER(C.c_double)]),
+            "prrtc_work_counters": (C.c_int, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.c_int]),
+            "prrtc_batch_settings_default": (None, [C.POINTER(BatchSettings)]),
+            "prrtc_batch_create": (C.c_int, [vp, C.c_int, C.POINTER(_Query), C.c_int, C.POINTER(BatchSettings), C.POINTER(vp)]),
+            "prrtc_batch_run": (C.c_int, [vp, vp]),
+            "prrtc_batch_results": (C.c_int, [vp, vp, C.POINTER(_Result)]),
+            "prrtc_batch_stats_get": (C.c_int, [vp, vp, C.POINTER(_BatchStats)]),
+            "prrtc_batch_free": (C.c_int, [vp, vp]),
+            "prrtc_solve_batch": (C.c_int, [vp, C.c_int, C.POINTER(_Query), C.c_int, C.POINTER(BatchSettings), C.POINTER(_Result)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -193,6 +228,18 @@ class Context:
     def launches(self) -> int:
         return int(lib().prrtc_launch_count(self.handle))
 
+    def measure_fp32_peak(self) -> float:
+        """FP32 FMA throughput of the device, TFLOP/s."""
+        v = C.c_double()
+        self._check(lib().prrtc_measure_fp32_peak(self.handle, C.byref(v)))
+        return v.value
+
+    def work_counters(self, reset: bool = False) -> tuple:
+        """(algorithmic FLOPs, configurations) checked since the last reset."""
+        f, n = C.c_uint64(), C.c_uint64()
+        self._check(lib().prrtc_work_counters(self.handle, C.byref(f), C.byref(n), int(reset)))
+        return f.value, n.value
+
     def set_planning_margin(self, pad: float):
         self._check(lib().prrtc_set_planning_margin(self.handle, pad))
 
@@ -200,13 +247,7 @@ class Context:
         self._check(lib().prrtc_set_time_budget(self.handle, int(ns)))
 
     def upload_env(self, env: Environment) -> EnvHandle:
-        d = EnvDesc()
-        keep = []
-        for k in ("spheres", "capsules", "z_aligned_capsules", "cylinders", "cuboids", "z_aligned_cuboids"):
-            a = np.ascontiguousarray(getattr(env, k), np.float32)
-            keep.append(a)
-            setattr(d, k, a.ctypes.data_as(C.POINTER(C.c_float)) if len(a) else None)
-            setattr(d, "num_" + k, len(a))
+        d, keep = _env_desc(env)
         h = C.c_void_p()
         self._check(lib().prrtc_env_upload(self.handle, C.byref(d), C.byref(h)))
         return EnvHandle(self, h, env)
@@ -250,6 +291,42 @@ class Context:
         self._check(lib().prrtc_fk_spheres(self.handle, rid, pq, n, po))
         return out
 
+    def batch(self, robot, queries, settings: BatchSettings | None = None, path_capacity: int = 4096) -> Batch:
+        """Prepare a batch; queries are (env, start, goals) tuples or objects
+        with env/start/goal attributes (env: Environment or EnvHandle)."""
+        return Batch(self, robot, queries, settings if settings is not None else BatchSettings(), path_capacity)
+
+    def solve_batch(self, robot, queries, settings: BatchSettings | None = None, path_capacity: int = 4096) -> list:
+        """prrtc_solve_batch: upload, solve and download in one call."""
+        rid = robot_id(robot)
+        b = Batch.__new__(Batch)
+        b.ctx, b.rid, b.D, b.n, b.path_capacity = self, rid, dof(rid), len(queries), path_capacity
+        b.handle = None
+        keep = []
+        qs = (_Query * b.n)()
+        for i, q in enumerate(queries):
+            env, start, goals = q if isinstance(q, tuple) else (q.env, q.start, q.goal)
+            start = np.ascontiguousarray(np.asarray(start, np.float32).reshape(b.D))
+            goals = np.ascontiguousarray(np.asarray(goals, np.float32).reshape(-1, b.D))
+            keep += [start, goals]
+            if isinstance(env, EnvHandle):
+                qs[i].env = env.handle
+            else:
+                d, k = _env_desc(env)
+                keep += [d, k]
+                qs[i].env_desc = C.cast(C.pointer(d), C.c_void_p)
+            qs[i].start, qs[i].goals, qs[i].num_goals = start.ctypes.data, goals.ctypes.data, len(goals)
+        res = (_Result * b.n)()
+        paths = np.empty((b.n, path_capacity, b.D), np.float32)
+        for i in range(b.n):
+            res[i].path_capacity = path_capacity
+            res[i].path = paths[i].ctypes.data_as(C.POINTER(C.c_float))
+        s = settings if settings is not None else BatchSettings()
+        self._check(lib().prrtc_solve_batch(self.handle, rid, qs, b.n, C.byref(s), res))
+        return [PlannerResult(bool(r.solved), paths[i, :r.path_rows].copy(), r.start_tree_size, r.goal_tree_size,
+                              r.path_length, r.iters, r.cost, r.wall_ns, r.kernel_ns, r.copy_ns, r.status)
+                for i, r in enumerate(res)]
+
     def solve(self, robot, start, goals, env, settings: Settings | None = None, path_capacity: int = 70000) -> PlannerResult:
         """pRRTC::solve<Robot>(start, goals, env, settings)."""
         rid = robot_id(robot)
@@ -269,6 +346,81 @@ class Context:
         return PlannerResult(bool(r.solved), path[:r.path_rows].copy() if r.solved else np.zeros((0, D), np.float32),
                              r.start_tree_size, r.goal_tree_size, r.path_length, r.iters, r.cost, r.wall_ns,
                              r.kernel_ns, r.copy_ns, r.status)
+
+
+class Batch:
+    """A prepared batch (prrtc_batch_create): run() solves every query in one
+    persistent launch with inputs resident on the device; results() copies
+    answers and paths back."""
+
+    def __init__(self, ctx: "Context", robot, queries, settings: BatchSettings, path_capacity: int = 4096):
+        self.ctx, self.rid = ctx, robot_id(robot)
+        self.D = dof(self.rid)
+        self.n = len(queries)
+        self.path_capacity = path_capacity
+        self._keep = []
+        qs = (_Query * self.n)()
+        for i, q in enumerate(queries):
+            env, start, goals = q if isinstance(q, tuple) else (q.env, q.start, q.goal)
+            start = np.ascontiguousarray(np.asarray(start, np.float32).reshape(self.D))
+            goals = np.ascontiguousarray(np.asarray(goals, np.float32).reshape(-1, self.D))
+            self._keep += [start, goals]
+            if isinstance(env, EnvHandle):
+                qs[i].env = env.handle
+            else:
+                d, keep = _env_desc(env)
+                self._keep += [d, keep]
+                qs[i].env_desc = C.cast(C.pointer(d), C.c_void_p)
+            qs[i].start = start.ctypes.data
+            qs[i].goals = goals.ctypes.data
+            qs[i].num_goals = len(goals)
+        self.settings = settings
+        h = C.c_void_p()
+        ctx._check(lib().prrtc_batch_create(ctx.handle, self.rid, qs, self.n, C.byref(settings), C.byref(h)))
+        self.handle = h
+        self._qs = qs
+
+    def run(self):
+        self.ctx._check(lib().prrtc_batch_run(self.ctx.handle, self.handle))
+
+    def results(self) -> list:
+        res = (_Result * self.n)()
+        paths = np.empty((self.n, self.path_capacity, self.D), np.float32)
+        for i in range(self.n):
+            res[i].path_capacity = self.path_capacity
+            res[i].path = paths[i].ctypes.data_as(C.POINTER(C.c_float))
+        self.ctx._check(lib().prrtc_batch_results(self.ctx.handle, self.handle, res))
+        return [PlannerResult(bool(r.solved), paths[i, :r.path_rows].copy(), r.start_tree_size, r.goal_tree_size,
+                              r.path_length, r.iters, r.cost, r.wall_ns, r.kernel_ns, r.copy_ns, r.status)
+                for i, r in enumerate(res)]
+
+    def stats(self) -> dict:
+        st = _BatchStats()
+        self.ctx._check(lib().prrtc_batch_stats_get(self.ctx.handle, self.handle, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in _BatchStats._fields_}
+
+    def free(self):
+        if getattr(self, "handle", None):
+            lib().prrtc_batch_free(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            if self.ctx.handle:
+                self.free()
+        except Exception:
+            pass
+
+
+def _env_desc(env: Environment):
+    d = EnvDesc()
+    keep = []
+    for k in ("spheres", "capsules", "z_aligned_capsules", "cylinders", "cuboids", "z_aligned_cuboids"):
+        a = np.ascontiguousarray(getattr(env, k), np.float32)
+        keep.append(a)
+        setattr(d, k, a.ctypes.data_as(C.POINTER(C.c_float)) if len(a) else None)
+        setattr(d, "num_" + k, len(a))
+    return d, keep
 
 
 def _empty_like_device(t, shape, dtype: str):

@@ -122,6 +122,22 @@ prrtc_status Ctx::device_view(const void *p, size_t bytes, int slot, bool in, vo
 
 // ---------------------------------------------------------------- C ABI
 
+// 8 independent FMA chains per thread: enough ILP to fill the FP32 pipe.
+__global__ void k_fma_peak(float *out, int iters, float a, float b)
+{
+    float x[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) x[i] = threadIdx.x * 1e-7f + i;
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) x[i] = fmaf(x[i], a, b);
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 8; i++) s += x[i];
+    if (s == 12345.0f) out[0] = s;   // keeps the chains live
+}
+
 extern "C" {
 
 const char *prrtc_status_string(prrtc_status s)
@@ -149,7 +165,9 @@ prrtc_status prrtc_create(prrtc_ctx **out, int device)
     Ctx *c = new Ctx();
     c->device = device;
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+        cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaMalloc(&c->work_dev, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMemset(c->work_dev, 0, 2 * sizeof(unsigned long long)) != cudaSuccess) {
         cudaGetLastError();
         delete c;
         return PRRTC_ECUDA;
@@ -169,6 +187,8 @@ prrtc_status prrtc_destroy(prrtc_ctx *ctx)
         for (auto &b : c->bufs)
             if (b.ptr) cudaFree(b.ptr);
         c->release_planner_state();
+        release_arena(c);
+        cudaFree(c->work_dev);
         cudaStreamDestroy(c->stream);
     }
     delete c;
@@ -295,7 +315,7 @@ prrtc_status prrtc_validate_configs(prrtc_ctx *ctx, prrtc_robot robot, const prr
     prrtc_status s;
     if ((s = c->device_view(q, sizeof(float) * ops->dof * n, 0, true, &dq))) return s;
     if ((s = c->device_view(out_free, n, 1, false, &dout))) return s;
-    LaunchEnv le{e->dev, e->counts, c->sms};
+    LaunchEnv le{e->dev, e->counts, c->sms, c->work_dev};
     if ((s = c->cuda(ops->validate_configs(le, (const float *)dq, n, (uint8_t *)dout, c->stream), "validate_configs launch"))) return s;
     c->launches++;
     if (dout != out_free && (s = c->cuda(cudaMemcpyAsync(out_free, dout, n, cudaMemcpyDeviceToHost, c->stream), "copy out"))) return s;
@@ -319,7 +339,7 @@ prrtc_status prrtc_validate_edges(prrtc_ctx *ctx, prrtc_robot robot, const prrtc
     if ((s = c->device_view(a, cb, 0, true, &da))) return s;
     if ((s = c->device_view(b, cb, 2, true, &db))) return s;
     if ((s = c->device_view(out_free, n, 1, false, &dout))) return s;
-    LaunchEnv le{e->dev, e->counts, c->sms};
+    LaunchEnv le{e->dev, e->counts, c->sms, c->work_dev};
     if ((s = c->cuda(ops->validate_edges(le, (const float *)da, (const float *)db, n, granularity, (uint8_t *)dout, c->stream),
                      "validate_edges launch")))
         return s;
@@ -345,6 +365,51 @@ prrtc_status prrtc_fk_spheres(prrtc_ctx *ctx, prrtc_robot robot, const float *q,
     c->launches++;
     if (dout != out && (s = c->cuda(cudaMemcpyAsync(out, dout, ob, cudaMemcpyDeviceToHost, c->stream), "copy out"))) return s;
     return c->cuda(cudaStreamSynchronize(c->stream), "fk_spheres");
+}
+
+prrtc_status prrtc_work_counters(prrtc_ctx *ctx, uint64_t *flops, uint64_t *configs, int reset)
+{
+    Ctx *c = Ctx::of(ctx);
+    if (!c) return PRRTC_EINVAL;
+    std::lock_guard<std::mutex> g(c->mu);
+    cudaSetDevice(c->device);
+    unsigned long long h[2];
+    prrtc_status s;
+    if ((s = c->cuda(cudaMemcpyAsync(h, c->work_dev, sizeof h, cudaMemcpyDeviceToHost, c->stream), "work counters")) ||
+        (reset && (s = c->cuda(cudaMemsetAsync(c->work_dev, 0, sizeof h, c->stream), "work counters"))) ||
+        (s = c->cuda(cudaStreamSynchronize(c->stream), "work counters")))
+        return s;
+    if (flops) *flops = h[0];
+    if (configs) *configs = h[1];
+    return PRRTC_OK;
+}
+
+prrtc_status prrtc_measure_fp32_peak(prrtc_ctx *ctx, double *tflops)
+{
+    Ctx *c = Ctx::of(ctx);
+    if (!c || !tflops) return PRRTC_EINVAL;
+    std::lock_guard<std::mutex> g(c->mu);
+    cudaSetDevice(c->device);
+    float *sink = (float *)c->scratch(3, 64);
+    if (!sink) return c->fail(PRRTC_ENOMEM, "fp32 peak: scratch");
+    const int threads = 256, blocks = c->sms * 8, iters = 4096;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    k_fma_peak<<<blocks, threads, 0, c->stream>>>(sink, iters, 0.999999f, 1e-6f);   // warm-up
+    cudaEventRecord(e0, c->stream);
+    for (int r = 0; r < 5; r++) k_fma_peak<<<blocks, threads, 0, c->stream>>>(sink, iters, 0.999999f, 1e-6f);
+    cudaEventRecord(e1, c->stream);
+    prrtc_status s = c->cuda(cudaEventSynchronize(e1), "fp32 peak");
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s) return s;
+    c->launches += 6;
+    const double flops = 5.0 * blocks * threads * (double)iters * 8 * 2;
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    return PRRTC_OK;
 }
 
 void prrtc_settings_default(prrtc_settings *s)

@@ -61,6 +61,10 @@ struct Ctx {
     };
     Buf bufs[4];
     PlannerState *planner = nullptr;
+    float *bases = nullptr;                 // Halton prime bases per sampling lane [lanes][16]
+    int bases_lanes = 0;
+    struct Arena *arena = nullptr;          // batched-planner arena kept between batches
+    unsigned long long *work_dev = nullptr; // [2] FLOPs, configurations (prrtc_work_counters)
     float plan_pad = 0.0f;                  // prrtc_set_planning_margin
     unsigned long long budget_ns = 0;       // prrtc_set_time_budget
 
@@ -74,6 +78,8 @@ struct Ctx {
 };
 
 const RobotOps *robot_ops(prrtc_robot r);
+prrtc_status ensure_halton_bases(Ctx *c, int lanes);
+void release_arena(Ctx *c);
 
 struct Limits;
 const Limits *robot_limits(prrtc_robot r);

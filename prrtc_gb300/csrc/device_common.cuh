@@ -92,28 +92,45 @@ __device__ __forceinline__ bool hit_z_cuboid(float4 c0, float4 c1, float4 c2, fl
     return a1 * a1 + a2 * a2 + a3 * a3 - rsq < 0.0f;
 }
 
+// Algorithmic FLOPs of one primitive test (FMA = 2; min/max/abs not counted),
+// the weights the roofline uses for the reference checker's work.
+constexpr int kFlopSphere = 11, kFlopCapsule = 26, kFlopZCapsule = 16, kFlopCuboid = 27, kFlopZCuboid = 18,
+              kFlopPair = 11;
+
 // Sphere against every obstacle with early exit
 // (sphere_environment_in_collision, utils.cuh:211-242).  Not inlined: every
-// generated call site shares one copy of the obstacle loops.
-static __device__ __noinline__ bool env_hit(const EnvView e, float x, float y, float z, float r)
+// generated call site shares one copy of the obstacle loops.  Returns
+// 2 * (FLOPs of the tests executed) + (1 if hit).
+static __device__ __noinline__ int env_hit(const EnvView e, float x, float y, float z, float r)
 {
     const float4 *p = e.rec;
-    for (int i = 0; i < e.n.ns; i++)
-        if (hit_sphere(p[i], x, y, z, r)) return true;
+    int w = 0;
+    for (int i = 0; i < e.n.ns; i++) {
+        w += kFlopSphere;
+        if (hit_sphere(p[i], x, y, z, r)) return 2 * w + 1;
+    }
     p += e.n.ns;
-    for (int i = 0; i < e.n.nc; i++)
-        if (hit_capsule(p[2 * i], p[2 * i + 1], x, y, z, r)) return true;
+    for (int i = 0; i < e.n.nc; i++) {
+        w += kFlopCapsule;
+        if (hit_capsule(p[2 * i], p[2 * i + 1], x, y, z, r)) return 2 * w + 1;
+    }
     p += 2 * e.n.nc;
-    for (int i = 0; i < e.n.nzc; i++)
-        if (hit_z_capsule(p[2 * i], p[2 * i + 1], x, y, z, r)) return true;
+    for (int i = 0; i < e.n.nzc; i++) {
+        w += kFlopZCapsule;
+        if (hit_z_capsule(p[2 * i], p[2 * i + 1], x, y, z, r)) return 2 * w + 1;
+    }
     p += 2 * e.n.nzc;
     const float rsq = r * r;
-    for (int i = 0; i < e.n.ncb; i++)
-        if (hit_cuboid(p[4 * i], p[4 * i + 1], p[4 * i + 2], p[4 * i + 3], x, y, z, rsq)) return true;
+    for (int i = 0; i < e.n.ncb; i++) {
+        w += kFlopCuboid;
+        if (hit_cuboid(p[4 * i], p[4 * i + 1], p[4 * i + 2], p[4 * i + 3], x, y, z, rsq)) return 2 * w + 1;
+    }
     p += 4 * e.n.ncb;
-    for (int i = 0; i < e.n.nzb; i++)
-        if (hit_z_cuboid(p[4 * i], p[4 * i + 1], p[4 * i + 2], x, y, z, rsq)) return true;
-    return false;
+    for (int i = 0; i < e.n.nzb; i++) {
+        w += kFlopZCuboid;
+        if (hit_z_cuboid(p[4 * i], p[4 * i + 1], p[4 * i + 2], x, y, z, rsq)) return 2 * w + 1;
+    }
+    return 2 * w;
 }
 
 __device__ __forceinline__ void xform(const Frame &T, float4 c, float &x, float &y, float &z)
@@ -123,24 +140,27 @@ __device__ __forceinline__ void xform(const Frame &T, float4 c, float &x, float 
     z = T.m[8] * c.x + T.m[9] * c.y + T.m[10] * c.z + T.m[11];
 }
 
-// Leaf spheres (given in frame T) against the environment; true on first hit.
-// pad inflates every radius (0 reproduces the reference exactly).
-static __device__ __noinline__ bool env_leaves(const EnvView e, const Frame T, const float4 *__restrict__ leaves, int n,
-                                        float pad)
+// Leaf spheres (given in frame T) against the environment; pad inflates every
+// radius (0 reproduces the reference exactly).  Returns 2 * FLOPs + (1 if any hit).
+static __device__ __noinline__ int env_leaves(const EnvView e, const Frame T, const float4 *__restrict__ leaves, int n,
+                                              float pad)
 {
+    int w = 0;
     for (int i = 0; i < n; i++) {
         const float4 c = __ldg(leaves + i);
         float x, y, z;
         xform(T, c, x, y, z);
-        if (env_hit(e, x, y, z, c.w + pad)) return true;
+        const int h = env_hit(e, x, y, z, c.w + pad);
+        w += h >> 1;
+        if (h & 1) return 2 * w + 1;
     }
-    return false;
+    return 2 * w;
 }
 
-// Leaf pairs: a in frame A, b in frame B, Tab = inv(T_A) * T_B; true when any
-// pair overlaps (sphere_sphere_self_collision, utils.cuh:83-86).  pad2 is the
-// added inflation of a pair (twice the per-sphere pad).
-static __device__ __noinline__ bool self_pairs(const Frame Tab, const LeafPair *__restrict__ pairs, int n, float pad2)
+// Leaf pairs: a in frame A, b in frame B, Tab = inv(T_A) * T_B
+// (sphere_sphere_self_collision, utils.cuh:83-86).  pad2 is the added
+// inflation of a pair (twice the per-sphere pad).  Returns 2 * FLOPs + hit.
+static __device__ __noinline__ int self_pairs(const Frame Tab, const LeafPair *__restrict__ pairs, int n, float pad2)
 {
     for (int i = 0; i < n; i++) {
         const float4 a = __ldg(&pairs[i].a);
@@ -149,33 +169,41 @@ static __device__ __noinline__ bool self_pairs(const Frame Tab, const LeafPair *
         xform(Tab, b, x, y, z);
         const float dx = a.x - x, dy = a.y - y, dz = a.z - z;
         const float rs = a.w + b.w + pad2;
-        if (dx * dx + dy * dy + dz * dz - rs * rs < 0.0f) return true;
+        if (dx * dx + dy * dy + dz * dz - rs * rs < 0.0f) return 2 * kFlopPair * (i + 1) + 1;
     }
-    return false;
+    return 2 * kFlopPair * n;
 }
 
 // What the generated checkers call.  pad = 0 and stop_flag = nullptr give the
 // reference checker's verdicts; planners may inflate every sphere by pad
-// (a certified margin) and share a block flag through which any lane's
-// collision ends the other lanes' work on the same edge.
+// (a certified margin) and share a flag through which any lane's collision
+// ends the other lanes' work on the same edge.  `work` accumulates the
+// algorithmic FLOPs of the primitive tests executed (reference weights).
 struct CheckCtx {
     EnvView env;
     float pad;
     volatile int *stop_flag;
-    __device__ __forceinline__ bool env_hit(float x, float y, float z, float r) const
+    unsigned work = 0;
+    __device__ __forceinline__ bool take(int h)
     {
-        return prrtc::env_hit(env, x, y, z, r + pad);
+        work += (unsigned)(h >> 1);
+        return h & 1;
     }
-    __device__ __forceinline__ bool env_leaves(const Frame &T, const float4 *l, int n) const
+    __device__ __forceinline__ bool env_hit(float x, float y, float z, float r)
     {
-        return prrtc::env_leaves(env, T, l, n, pad);
+        return take(prrtc::env_hit(env, x, y, z, r + pad));
     }
-    __device__ __forceinline__ bool self_pairs(const Frame &T, const LeafPair *p, int n) const
+    __device__ __forceinline__ bool env_leaves(const Frame &T, const float4 *l, int n)
     {
-        return prrtc::self_pairs(T, p, n, 2.0f * pad);
+        return take(prrtc::env_leaves(env, T, l, n, pad));
     }
-    __device__ __forceinline__ bool pair_hit(float dx, float dy, float dz, float rs) const
+    __device__ __forceinline__ bool self_pairs(const Frame &T, const LeafPair *p, int n)
     {
+        return take(prrtc::self_pairs(T, p, n, 2.0f * pad));
+    }
+    __device__ __forceinline__ bool pair_hit(float dx, float dy, float dz, float rs)
+    {
+        work += kFlopPair;
         rs += 2.0f * pad;
         return dx * dx + dy * dy + dz * dz - rs * rs < 0.0f;
     }

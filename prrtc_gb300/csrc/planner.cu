@@ -29,8 +29,6 @@ struct PlannerState {
     float *radii = nullptr;     // [2][cap]
     float *path = nullptr;      // [2][path_cap][dof]
     QueryCtl *ctl = nullptr;
-    float *bases = nullptr;     // [lanes][16]
-    int lanes = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -66,13 +64,33 @@ static void free_state(PlannerState *p)
     cudaFree(p->radii);
     cudaFree(p->path);
     cudaFree(p->ctl);
-    cudaFree(p->bases);
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
 }
 
+prrtc_status ensure_halton_bases(Ctx *c, int lanes)
+{
+    if (c->bases_lanes >= lanes) return PRRTC_OK;
+    cudaFree(c->bases);
+    c->bases = nullptr;
+    c->bases_lanes = 0;
+    const int want = std::max(lanes, 1024);
+    if (cudaMalloc(&c->bases, sizeof(float) * 16 * want) != cudaSuccess) {
+        cudaGetLastError();
+        return c->fail(PRRTC_ENOMEM, "cannot allocate Halton bases");
+    }
+    prrtc_status s = c->cuda(launch_halton_bases(c->bases, want, c->stream), "halton bases");
+    if (s) return s;
+    c->launches++;
+    c->bases_lanes = want;
+    return PRRTC_OK;
+}
+
 void Ctx::release_planner_state()
 {
+    cudaFree(bases);
+    bases = nullptr;
+    bases_lanes = 0;
     if (planner) {
         free_state(planner);
         delete planner;
@@ -118,20 +136,6 @@ static prrtc_status ensure_state(Ctx *c, int dof, int cap, int lanes)
         cudaGetLastError();
         return c->fail(PRRTC_ENOMEM, "solve: cannot allocate control block");
     }
-    if (p->lanes < lanes) {
-        cudaFree(p->bases);
-        p->bases = nullptr;
-        p->lanes = 0;
-        const int want = std::max(lanes, 1024);
-        if (cudaMalloc(&p->bases, sizeof(float) * 16 * want) != cudaSuccess) {
-            cudaGetLastError();
-            return c->fail(PRRTC_ENOMEM, "solve: cannot allocate Halton bases");
-        }
-        prrtc_status s = c->cuda(launch_halton_bases(p->bases, want, c->stream), "halton bases");
-        if (s) return s;
-        c->launches++;
-        p->lanes = want;
-    }
     return PRRTC_OK;
 }
 
@@ -165,6 +169,7 @@ extern "C" prrtc_status prrtc_solve(prrtc_ctx *ctx, prrtc_robot robot, const flo
     const int cap = (S.max_samples + 3) & ~3;
     prrtc_status s = ensure_state(c, D, cap, S.num_new_configs);
     if (s) return s;
+    if ((s = ensure_halton_bases(c, S.num_new_configs))) return s;
     PlannerState *p = c->planner;
     cudaStream_t st = c->stream;
 
@@ -222,13 +227,14 @@ extern "C" prrtc_status prrtc_solve(prrtc_ctx *ctx, prrtc_robot robot, const flo
     P.radii[0] = rad0;
     P.radii[1] = rad1;
     P.cap = p->cap;
-    P.halton_bases = p->bases;
+    P.halton_bases = c->bases;
     prrtc_robot_limits(robot, P.scale, P.offset);
     P.env = e->dev;
     P.env_n = e->counts;
     P.ctl = p->ctl;
     P.path = p->path;
     P.path_cap = p->path_cap;
+    P.work = c->work_dev;
     int threads = ((S.granularity + 31) / 32) * 32;
     if (threads > 256) threads = 256;
 

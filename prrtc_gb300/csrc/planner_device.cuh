@@ -163,3 +163,67 @@ __device__ int trace_to_root(const float *nodes, const int *parents, int cap, in
 }
 
 }  // namespace prrtc
+
+namespace prrtc {
+
+// ---------------------------------------------------------------------------
+// Warp-level pieces for the batched planner: every warp is an independent
+// worker, so nothing here synchronises more than one warp.
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+// Warp argmin of squared distance from q (all lanes hold the full q) over the
+// first `count` nodes of a SoA tree; ties -> lowest index.  All lanes return
+// the result.
+template <int D>
+__device__ __forceinline__ void warp_nn(const float *__restrict__ nodes, int cap, int count, const float (&q)[D],
+                                        float &out_d, int &out_i)
+{
+    float bd = FLT_MAX;
+    int bi = 0x7fffffff;
+    if (count > cap) count = cap;
+    const int n4 = (count + 3) >> 2;
+    const float4 *base = reinterpret_cast<const float4 *>(nodes);
+    const int cap4 = cap >> 2;
+    for (int c = lane_id(); c < n4; c += 32) {
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            const float4 v = __ldcg(base + (size_t)d * cap4 + c);
+            const float x0 = v.x - q[d], x1 = v.y - q[d], x2 = v.z - q[d], x3 = v.w - q[d];
+            a0 = fmaf(x0, x0, a0);
+            a1 = fmaf(x1, x1, a1);
+            a2 = fmaf(x2, x2, a2);
+            a3 = fmaf(x3, x3, a3);
+        }
+        const int i0 = 4 * c;
+        if (a0 < bd) { bd = a0; bi = i0; }
+        if (a1 < bd) { bd = a1; bi = i0 + 1; }
+        if (a2 < bd) { bd = a2; bi = i0 + 2; }
+        if (a3 < bd) { bd = a3; bi = i0 + 3; }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float od = __shfl_xor_sync(0xffffffffu, bd, off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (od < bd || (od == bd && oi < bi)) { bd = od; bi = oi; }
+    }
+    out_d = bd;
+    out_i = bi == 0x7fffffff ? 0 : bi;
+}
+
+// Radical inverse of index i in integer base b, float32 (the closed form of
+// the reference's incremental Halton recurrence).
+__device__ __forceinline__ float radical_inverse(unsigned i, unsigned b)
+{
+    const float inv = 1.0f / (float)b;
+    float f = inv, r = 0.0f;
+    while (i > 0) {
+        r = fmaf(f, (float)(i % b), r);
+        i /= b;
+        f *= inv;
+    }
+    return r;
+}
+
+}  // namespace prrtc

@@ -15,6 +15,7 @@ struct LaunchEnv {
     const float4 *rec;   // device records
     EnvCounts counts;
     int sms;             // SM count of the device
+    unsigned long long *work;   // [2]: FLOPs, configurations (device, accumulated)
 };
 
 // Device control block of one query (replaces the reference's file-scope
@@ -54,6 +55,78 @@ struct PlainParams {
     QueryCtl *ctl;
     float *path;                       // [2][path_cap][dof]
     int path_cap;
+    unsigned long long *work;          // [2]: FLOPs, configurations (device, accumulated)
+};
+
+// ---- batched planner ------------------------------------------------------
+struct BatchQueryDesc {
+    const float4 *env;   // packed obstacle records (device)
+    EnvCounts env_n;
+    int cfg_off;         // float offset of start (dof floats) then goals in the config pool
+    int num_goals;
+};
+
+enum SlotStateCode { SLOT_FREE = 0, SLOT_RUNNING = 1, SLOT_DONE = 2, SLOT_BUSY = 3 };
+
+// One resident query slot (its trees live in the arena at the slot's index).
+struct SlotState {
+    int query;
+    int state;           // SlotStateCode
+    int free_index[2];
+    int ticket;          // samples drawn so far
+    int workers;         // warps registered on the slot
+    int pad_[2];
+};
+
+// Per-query result, written by the warp that finishes the query.
+struct BatchOut {
+    int solved;          // 1 solved, 0 not
+    int status;          // 0 ok, prrtc_status otherwise
+    int start_tree_size, goal_tree_size;
+    int path_length;
+    int iters;
+    float cost;
+    int path_off, path_rows;
+    int reached_goal;
+    int samples;
+    int pad_;
+    unsigned long long t_admit, t_done;   // device globaltimer, ns
+};
+
+struct BatchCounters {
+    int admit_next;      // next query to admit
+    int cursor;          // round-robin slot cursor
+    int done;            // queries finished
+    int path_next;       // rows used in the path pool
+    int error;           // bit 0: a worker gave up waiting for work
+    int pad_[3];
+    unsigned long long t0;
+    unsigned long long work[2];      // algorithmic FLOPs of the checks, configurations checked
+    unsigned long long nn_nodes;     // tree nodes visited by nearest-neighbour scans
+};
+
+struct BatchParams {
+    int max_samples, max_iters, lanes, granularity;
+    float range;
+    int balance;
+    float tree_ratio;
+    int dynamic_domain;
+    float dd_alpha, dd_radius, dd_min_radius;
+    float pad;
+    unsigned long long budget_ns;
+    int num_queries, num_slots, cap, path_pool_rows;
+    const float *cfg_pool;
+    const BatchQueryDesc *queries;
+    SlotState *slots;
+    BatchOut *out;
+    BatchCounters *ctr;
+    float *nodes;        // [slot][2][dof][cap], NaN where unwritten
+    int *parents;        // [slot][2][cap]
+    float *radii;        // [slot][2][cap]
+    int *tsel;           // [slot][lanes] balance-2 tree choice per virtual lane
+    float *path_pool;    // [path_pool_rows][dof]
+    const float *halton_bases;   // [lanes][16]
+    float scale[16], offset[16];
 };
 
 struct RobotOps {
@@ -64,6 +137,8 @@ struct RobotOps {
                                   uint8_t *out, cudaStream_t);
     cudaError_t (*fk_spheres)(const float *q, int64_t n, float *out, int sms, cudaStream_t);
     cudaError_t (*solve_plain)(const PlainParams &, int threads, cudaStream_t);
+    cudaError_t (*solve_batch)(const BatchParams &, int blocks, int warps_per_block, cudaStream_t);
+    int (*batch_occupancy)(int warps_per_block);   // resident blocks per SM
 };
 
 // Shuffled Halton prime bases per sampling lane, as the reference seeds them

@@ -356,6 +356,8 @@ def emit_cuda_checker(m: dict) -> str:
     w(f"constexpr int kNumSpheres = {len(sp)};")
     w(f"constexpr int kNumLeaves = {max(1, len(leaf_rows))};")
     w(f"constexpr int kNumPairs = {max(1, len(pair_rows))};")
+    w("// canonical algorithmic FLOPs of one forward kinematics: 2 * (12 * dof + 9 * spheres)")
+    w(f"constexpr unsigned kFkFlops = {2 * (12 * m['dof'] + 9 * len(sp))}u;")
     w("")
     w("// leaf spheres in their frame: (x, y, z, r)")
     w(f"__device__ const float4 k{R}Leaf[kNumLeaves] = {{")

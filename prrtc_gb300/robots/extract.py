@@ -264,12 +264,27 @@ def model_frames(model, q):
     return T
 
 
-def model_sphere_centres(model, q):
-    """(S, N, 3) float64 world centres of every model sphere."""
-    T = model_frames(model, q)
-    n = np.asarray(q).shape[0]
-    out = np.empty((len(model["spheres"]), n, 3))
-    for i, s in enumerate(model["spheres"]):
+def model_sphere_centres(model, q, only=None):
+    """(S, N, 3) float64 world centres of the model spheres (all, or the
+    indices in `only`, in that order)."""
+    q = np.asarray(q, dtype=np.float64)
+    idx = range(len(model["spheres"])) if only is None else list(only)
+    sph = [model["spheres"][i] for i in idx]
+    if only is not None:
+        needed = {s["frame"] for s in sph}
+        sub = dict(model)
+        keep = set()
+        parent = {jt["q"]: jt["parent"] for jt in model["joints"]}
+        for f in needed:
+            while f >= 0 and f not in keep:
+                keep.add(f)
+                f = parent[f]
+        sub["joints"] = [jt for jt in model["joints"] if jt["q"] in keep]
+        T = model_frames(sub, q)
+    else:
+        T = model_frames(model, q)
+    out = np.empty((len(sph), q.shape[0], 3))
+    for i, s in enumerate(sph):
         Tf = T[s["frame"]]
         out[i] = Tf[:, :3, :3] @ np.array(s["c"]) + Tf[:, :3, 3]
     return out

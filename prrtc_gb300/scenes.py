@@ -276,8 +276,9 @@ def hand_sphere(robot: str) -> int:
 
 
 def in_cell(robot: str, q: np.ndarray, cell) -> np.ndarray:
+    from .robots.extract import model_sphere_centres
     lo, hi = cell
-    c = sphere_centres(robot, q)[hand_sphere(robot)]
+    c = model_sphere_centres(load_model(robot), np.asarray(q, np.float64), only=[hand_sphere(robot)])[0]
     return np.all((c >= lo) & (c <= hi), axis=-1)
 
 

@@ -1,0 +1,95 @@
+"""Batched planner: many queries in one persistent launch.  Every returned
+path revalidates under the oracle at the planner's granularity; admission
+with fewer slots than queries, CUDA-graph replay, repeated runs and the time
+budget all keep that bar."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def c0(**kw):
+    from prrtc_gb300 import Settings
+    s = dict(max_samples=100000, max_iters=100000, num_new_configs=256, granularity=32, range=1.0, balance=0,
+             dynamic_domain=False)
+    s.update(kw)
+    return Settings(**s)
+
+
+def queries(robot, kind, n, seed0=0, nobs=None):
+    from prrtc_gb300 import scenes
+    return [scenes.make_query(robot, kind, seed0 + i, nobs) for i in range(n)]
+
+
+def check_all(oracle, robot, qs, res, g, need_all=True):
+    solved = 0
+    for q, r in zip(qs, res):
+        if not r.solved:
+            assert not need_all, r
+            continue
+        solved += 1
+        np.testing.assert_array_equal(r.path[0], q.goal)
+        np.testing.assert_array_equal(r.path[-1], q.start)
+        assert oracle.check_edges(robot, q.env, r.path[:-1], r.path[1:], g).all()
+    return solved
+
+
+def test_batch_tabletop(ctx, oracle):
+    from prrtc_gb300 import BatchSettings
+    qs = queries("panda", "tabletop", 64)
+    res = ctx.solve_batch("panda", qs, BatchSettings(c0()))
+    assert check_all(oracle, "panda", qs, res, 32) == 64
+
+
+def test_batch_shelf_dd_balance2(ctx, oracle):
+    from prrtc_gb300 import BatchSettings
+    qs = queries("panda", "shelf", 48)
+    s = c0(granularity=128, balance=2, tree_ratio=1.0, dynamic_domain=True, range=0.5)
+    res = ctx.solve_batch("panda", qs, BatchSettings(s))
+    assert check_all(oracle, "panda", qs, res, 128) == 48
+
+
+def test_batch_admission_graph_and_reruns(ctx, oracle):
+    from prrtc_gb300 import BatchSettings
+    qs = queries("fetch", "mixed", 40, 100, 20)
+    b = ctx.batch("fetch", qs, BatchSettings(c0(granularity=64, balance=1, tree_ratio=0.5), max_active=7, use_graph=1))
+    for _ in range(3):
+        b.run()
+        res = b.results()
+        assert check_all(oracle, "fetch", qs, res, 64) == 40
+        st = b.stats()
+        assert st["solved"] == 40 and st["error"] == 0 and st["slots"] == 7
+    b.free()
+
+
+def test_batch_baxter_mixed_difficulty(ctx, oracle):
+    from prrtc_gb300 import BatchSettings
+    from prrtc_gb300 import scenes
+    qs = [scenes.make_query("baxter", "tabletop" if i % 2 else "shelf", 200 + i, z_offset=0.3) for i in range(16)]
+    res = ctx.solve_batch("baxter", qs, BatchSettings(c0(granularity=128, balance=1, tree_ratio=0.5)))
+    assert check_all(oracle, "baxter", qs, res, 128, need_all=False) >= 12
+
+
+def test_batch_margin_paths_certified(ctx, oracle):
+    """With a planning margin every path's points clear contact by it."""
+    from prrtc_gb300 import BatchSettings
+    qs = queries("panda", "shelf", 16, 50)
+    res = ctx.solve_batch("panda", qs, BatchSettings(c0(granularity=32), margin=1e-4))
+    for q, r in zip(qs, res):
+        assert r.solved
+        a, b = r.path[:-1], r.path[1:]
+        step = (b - a) / np.float32(32)
+        pts = np.concatenate([a + np.float32(k) * step for k in range(1, 33)]).astype(np.float32)
+        assert oracle.clearance("panda", q.env, pts).min() > 5e-5
+
+
+def test_batch_time_budget_and_iteration_limit(ctx):
+    from prrtc_gb300 import BatchSettings
+    qs = queries("panda", "shelf", 32)
+    res = ctx.solve_batch("panda", qs, BatchSettings(c0(max_iters=1, num_new_configs=1)))
+    assert all((not r.solved and r.status == 0) or r.solved for r in res)
+    res = ctx.solve_batch("panda", qs, BatchSettings(c0(), max_active=4, time_budget_ns=1))
+    assert all(r.status == 3 for r in res if not r.solved)
+    # the arena is clean again: a normal batch still solves everything
+    res = ctx.solve_batch("panda", qs[:8], BatchSettings(c0()))
+    assert all(r.solved for r in res)

@@ -93,3 +93,25 @@ def test_device_pointers_and_edge_cases(ctx, oracle):
     big = Environment(cuboids=np.zeros((800, 15), np.float32))
     with pytest.raises(PrrtcError):
         ctx.upload_env(big)
+
+
+WEIGHTS = np.array([11, 26, 16, 27, 18, 11], np.int64)   # sphere, capsule, z-capsule, cuboid, z-cuboid, pair
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_work_counts_match_oracle(case, ctx, oracle):
+    """The checker's FLOP counter equals the oracle's executed-test count
+    (reference hierarchy and early exits) times the roofline weights, plus the
+    canonical FK count per configuration."""
+    robot = case.split("_")[0]
+    env, z = load_golden(case)
+    q = z["q"][z["margin"] > 1e-4]          # away from contact: identical test sequences
+    ctx.work_counters(reset=True)
+    ctx.validate_configs(robot, env, q)
+    flops, n = ctx.work_counters(reset=True)
+    _, counts = oracle.check(robot, env, q, counts=True)
+    from prrtc_gb300.scenes import load_model
+    m = load_model(robot)
+    fk = 2 * (12 * m["dof"] + 9 * len(m["spheres"]))
+    assert n == len(q)
+    assert flops == int(counts @ WEIGHTS) + fk * len(q)
