@@ -147,7 +147,7 @@ static __device__ __noinline__ int env_leaves(const EnvView e, const Frame T, co
 {
     int w = 0;
     for (int i = 0; i < n; i++) {
-        const float4 c = __ldg(leaves + i);
+        const float4 c = leaves[i];
         float x, y, z;
         xform(T, c, x, y, z);
         const int h = env_hit(e, x, y, z, c.w + pad);
@@ -163,8 +163,8 @@ static __device__ __noinline__ int env_leaves(const EnvView e, const Frame T, co
 static __device__ __noinline__ int self_pairs(const Frame Tab, const LeafPair *__restrict__ pairs, int n, float pad2)
 {
     for (int i = 0; i < n; i++) {
-        const float4 a = __ldg(&pairs[i].a);
-        const float4 b = __ldg(&pairs[i].b);
+        const float4 a = pairs[i].a;
+        const float4 b = pairs[i].b;
         float x, y, z;
         xform(Tab, b, x, y, z);
         const float dx = a.x - x, dy = a.y - y, dz = a.z - z;

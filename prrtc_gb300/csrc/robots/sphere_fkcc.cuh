@@ -37,7 +37,10 @@ __device__ __forceinline__ bool fkcc(const float *__restrict__ q, Ctx &ctx)
     const float t2_6 = a2_4;
     const float t2_7 = a2_5;
     const float t2_8 = q[2];
-    if (ctx.env_leaves(Frame{{1.0f, 0.0f, 0.0f, t2_6, 0.0f, 1.0f, 0.0f, t2_7, 0.0f, 0.0f, 1.0f, t2_8}}, kSphereLeaf + 0, 1)) return false;
+    const float p9 = t2_6;
+    const float p10 = t2_7;
+    const float p11 = t2_8;
+    if (ctx.env_hit(p9, p10, p11, 1.0f)) return false;
     if (ctx.stop()) return true;
     return true;
 }

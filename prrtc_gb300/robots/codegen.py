@@ -31,6 +31,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 CSRC = HERE.parent / "csrc" / "robots"
 ROBOTS = ("sphere", "panda", "fetch", "baxter")
+INLINE_LEAVES = 6   # leaf blocks up to this size are emitted as straight-line tests
 
 
 def load_model(robot: str) -> dict:
@@ -293,10 +294,19 @@ def emit_cuda_checker(m: dict) -> str:
         self_blocks[gi] = blocks
 
     def env_block_calls(gi):
+        """Leaf tests of an environment group: blocks of up to INLINE_LEAVES
+        spheres are tested inline (centres folded at generation time), larger
+        ones through ctx.env_leaves over the leaf table."""
         calls = []
         for f, first, n in env_blocks[gi]:
             T = fk.frame(f)
-            calls.append(f"ctx.env_leaves({_frame_arg(T)}, k{R}Leaf + {first}, {n})")
+            if n <= INLINE_LEAVES:
+                for k in range(first, first + n):
+                    x, y, z, r = leaf_rows[k]
+                    p = fk.point(f, (x, y, z))
+                    calls.append(f"ctx.env_hit({_op(p[0])}, {_op(p[1])}, {_op(p[2])}, {_lit(r)})")
+            else:
+                calls.append(f"ctx.env_leaves({_frame_arg(T)}, k{R}Leaf + {first}, {n})")
         return calls
 
     for kind, gi in m["schedule"]:

@@ -296,9 +296,20 @@ def make_query(robot: str, kind: str, seed: int, n_obstacles: int | None = None,
     rng = Rng(seed ^ 0x5A5A5A5A)
     start = sample_free(robot, env, rng)
     if kind == "shelf":
+        # goal: hand inside a random cell; a cell the hand cannot reach free of
+        # collision within the attempt budget gives way to the next draw
         cells = shelf_cells(z_offset)
-        cell = cells[rng.integers(0, 8)]
-        goal = sample_free(robot, env, rng, accept=lambda q: in_cell(robot, q, cell), batch=4096, max_batches=400)
+        goal = None
+        for _ in range(16):
+            cell = cells[rng.integers(0, 8)]
+            try:
+                goal = sample_free(robot, env, rng, accept=lambda q: in_cell(robot, q, cell), batch=4096,
+                                   max_batches=60)
+                break
+            except RuntimeError:
+                continue
+        if goal is None:
+            raise RuntimeError(f"no reachable shelf cell for {robot} seed {seed}")
     else:
         goal = sample_free(robot, env, rng)
     return Query(env, start, goal, seed, kind)
