@@ -159,8 +159,10 @@ def metric_name(args):
 
 
 def config_of(args):
+    from prrtc_gb300 import autotune, workloads
     return {"workload": f"{args.workload}_{args.queries}", "queries": args.queries,
             "settings": WORKLOAD_SETTINGS[args.workload], "planning_margin_m": MARGIN,
+            "batch_shape": autotune.load(workloads.WORKLOADS[args.workload][0], args.workload),
             "l2": "flushed between steps (256 MiB write)", "parallelism": "queries sharded over ranks"}
 
 
@@ -176,7 +178,7 @@ def h2d_bytes(qs):
 
 def ours(args, rank, world):
     import torch
-    from prrtc_gb300 import BatchSettings, Context, build, workloads
+    from prrtc_gb300 import BatchSettings, Context, autotune, build, workloads
     build.build()
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
@@ -185,7 +187,8 @@ def ours(args, rank, world):
     plan = settings_for(args.workload)
     ctx = Context(dev)
     envs = [ctx.upload_env(q.env) for q in qs]
-    bs = BatchSettings(plan, use_graph=1, margin=MARGIN, time_budget_ns=GPU_BUDGET_NS)
+    tuned = autotune.load(robot, args.workload)
+    bs = BatchSettings(plan, use_graph=1, margin=MARGIN, time_budget_ns=GPU_BUDGET_NS, **tuned)
     batch = ctx.batch(robot, [(e, q.start, q.goal) for e, q in zip(envs, qs)], bs, path_capacity=2048)
     flush = torch.empty(64 << 20, dtype=torch.float32, device=f"cuda:{dev}")
     launches0 = ctx.launches

@@ -202,10 +202,17 @@ typedef struct prrtc_query {
 } prrtc_query;
 
 typedef struct prrtc_batch_settings {
-    prrtc_settings plan;             /* applied to every query; num_new_configs = virtual sampling lanes */
-    int max_nodes_per_tree;          /* arena capacity per tree (0: min(max_samples, 16384)) */
+    prrtc_settings plan;             /* applied to every query (num_new_configs: see lanes) */
+    int lanes;                       /* virtual sampling lanes per query: sample k of a query is
+                                        Halton point k / lanes + 1 of lane k % lanes, and the balance
+                                        modes see the lane as pRRTC sees blockIdx.x.  0: 2.  pRRTC's
+                                        own count (plan.num_new_configs) reproduces its sample set,
+                                        whose first points cluster near the lower joint limits */
+    int max_nodes_per_tree;          /* arena capacity per tree (0: min(max_samples, 32768)) */
     int max_active;                  /* resident query slots (0: all queries, within the arena budget) */
     int warps_per_block;             /* 0: 4 */
+    int edge_order;                  /* order a warp checks an edge's points in: 0 contiguous
+                                        rounds, 1 interleaved (every round spans the edge) */
     int blocks_per_sm;               /* 0: occupancy maximum */
     int use_graph;                   /* replay each run as a captured CUDA graph */
     float margin;                    /* sphere inflation while planning, metres (>= 0) */

@@ -78,8 +78,9 @@ class _Query(C.Structure):
 class BatchSettings(C.Structure):
     """prrtc_batch_settings: planner settings for every query plus the batch's
     arena, launch shape, CUDA-graph and margin options."""
-    _fields_ = [("plan", Settings), ("max_nodes_per_tree", C.c_int), ("max_active", C.c_int),
-                ("warps_per_block", C.c_int), ("blocks_per_sm", C.c_int), ("use_graph", C.c_int),
+    _fields_ = [("plan", Settings), ("lanes", C.c_int), ("max_nodes_per_tree", C.c_int), ("max_active", C.c_int),
+                ("warps_per_block", C.c_int), ("edge_order", C.c_int), ("blocks_per_sm", C.c_int),
+                ("use_graph", C.c_int),
                 ("margin", C.c_float), ("time_budget_ns", C.c_uint64)]
 
     def __init__(self, plan: Settings | None = None, **kw):

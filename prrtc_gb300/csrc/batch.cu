@@ -137,13 +137,14 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     if (!ops || !queries || n < 1 || !settings || !out) return c->fail(PRRTC_EINVAL, "batch_create: bad argument");
     const prrtc_settings &S = settings->plan;
     if (S.num_new_configs < 1 || S.granularity < 1 || S.granularity > 1024 || !(S.range > 0.0f) || S.max_iters < 0 ||
-        !(settings->margin >= 0.0f) || settings->warps_per_block < 0 || settings->warps_per_block > 4)
+        !(settings->margin >= 0.0f) || settings->warps_per_block < 0 || settings->warps_per_block > 4 ||
+        settings->lanes < 0 || settings->lanes > 4096)
         return c->fail(PRRTC_EINVAL, "batch_create: bad settings");
     std::lock_guard<std::mutex> g(c->mu);
     cudaSetDevice(c->device);
     *out = nullptr;
     const int D = ops->dof;
-    int cap = settings->max_nodes_per_tree > 0 ? settings->max_nodes_per_tree : std::min(S.max_samples, 16384);
+    int cap = settings->max_nodes_per_tree > 0 ? settings->max_nodes_per_tree : std::min(S.max_samples, 32768);
     cap = std::max(4, (std::min(cap, S.max_samples) + 3) & ~3);
     // pack queries
     std::vector<float> cfg;
@@ -179,7 +180,7 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     b->n = n;
     b->dof = D;
     b->cap = cap;
-    b->lanes = S.num_new_configs;
+    b->lanes = settings->lanes > 0 ? settings->lanes : 2;
     b->use_graph = settings->use_graph != 0;
     b->wpb = settings->warps_per_block > 0 ? settings->warps_per_block : 4;
     const size_t slot_bytes = (size_t)2 * cap * (D + 2) * sizeof(float);
@@ -229,7 +230,7 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     BatchParams &P = b->P;
     P.max_samples = S.max_samples;
     P.max_iters = S.max_iters;
-    P.lanes = S.num_new_configs;
+    P.lanes = b->lanes;
     P.granularity = S.granularity;
     P.range = S.range;
     P.balance = S.balance;
@@ -244,6 +245,7 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     P.num_slots = slots;
     P.cap = cap;
     P.path_pool_rows = b->path_rows;
+    P.edge_order = settings->edge_order ? 1 : 0;
     P.cfg_pool = reinterpret_cast<const float *>(base + o_cfg);
     P.queries = reinterpret_cast<const BatchQueryDesc *>(base + o_desc);
     P.slots = reinterpret_cast<SlotState *>(base + o_slots);

@@ -115,6 +115,7 @@ struct BatchParams {
     float pad;
     unsigned long long budget_ns;
     int num_queries, num_slots, cap, path_pool_rows;
+    int edge_order;      // 0 contiguous, 1 interleaved (see warp_validate)
     const float *cfg_pool;
     const BatchQueryDesc *queries;
     SlotState *slots;

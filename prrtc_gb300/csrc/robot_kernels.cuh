@@ -345,10 +345,14 @@ struct WarpScratch {
     int pad_[3];
 };
 
-// Whole warp: check the g points of the edge in W (from + k * step); counts
-// the points examined into *checked (lane 0).
+// Whole warp: check the g points of the edge in W (from + k * step),
+// k = 1..g, in ceil(g / 32) rounds of one point per lane.  Contiguous order
+// gives round r the points 32 r + lane + 1; interleaved order gives it
+// lane * R + r + 1, so the first round already samples the whole edge at
+// stride R and a collision usually ends the edge after one round.  Adds the
+// work done to work[0] (FLOPs) and work[1] (points).
 template <class Gen>
-__device__ __forceinline__ bool warp_validate(const WarpScratch &W, int g, CheckCtx &ctx,
+__device__ __forceinline__ bool warp_validate(const WarpScratch &W, int g, int interleave, CheckCtx &ctx,
                                               unsigned long long *work)
 {
     constexpr int D = Gen::kDof;
@@ -359,8 +363,9 @@ __device__ __forceinline__ bool warp_validate(const WarpScratch &W, int g, Check
     bool bad = false;
     int n = 0;
     unsigned long long flops = 0;
-    for (int base = 0; base < g; base += 32) {
-        const int k = base + lane + 1;
+    const int R = (g + 31) >> 5;
+    for (int r = 0; r < R; r++) {
+        const int k = interleave ? lane * R + r + 1 : 32 * r + lane + 1;
         const bool run = k <= g && !*flag;
         if (run) {
             float q[D];
@@ -741,7 +746,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                     W.step[lane] = __fdiv_rn(__fsub_rn(c, nn), fg);
                 }
                 __syncwarp();
-                if (!warp_validate<Gen>(W, P.granularity, ctx, C->work)) {
+                if (!warp_validate<Gen>(W, P.granularity, P.edge_order, ctx, C->work)) {
                     if (lane == 0 && P.dynamic_domain) dd_shrink(rd_t + ni, P.dd_alpha, P.dd_radius, P.dd_min_radius);
                 } else {
                     int idx = -1;
@@ -784,7 +789,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                                 W.step[lane] = __fdiv_rn(__fsub_rn(b, a), fg);
                             }
                             __syncwarp();
-                            if (!warp_validate<Gen>(W, P.granularity, ctx, C->work)) break;
+                            if (!warp_validate<Gen>(W, P.granularity, P.edge_order, ctx, C->work)) break;
                             int idx2 = -1;
                             if (lane == 0) {
                                 idx2 = atomicAdd(&S->free_index[t], 1);

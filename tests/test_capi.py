@@ -37,3 +37,27 @@ def test_robot_tables():
     from prrtc_gb300 import api
     assert [api.dof(r) for r in ("sphere", "panda", "fetch", "baxter")] == [3, 7, 8, 14]
     assert [api.num_spheres(r) for r in ("sphere", "panda", "fetch", "baxter")] == [1, 69, 125, 100]
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """ctypes mirrors of the ABI structs have the header's size and offsets."""
+    import subprocess
+    from prrtc_gb300 import api
+    structs = {"prrtc_settings": api.Settings, "prrtc_result": api._Result, "prrtc_env_desc": api.EnvDesc,
+               "prrtc_query": api._Query, "prrtc_batch_settings": api.BatchSettings,
+               "prrtc_batch_stats": api._BatchStats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "prrtc/prrtc.h"', 'int main(void) {']
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname}.{f} %zu\\n", offsetof({cname}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", f"-I{ROOT / 'include'}", str(src), "-o", str(exe)], check=True)
+    got = dict(l.rsplit(" ", 1) for l in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n") if l)
+    for cname, py in structs.items():
+        assert int(got[cname]) == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert int(got[f"{cname}.{f}"]) == getattr(py, f).offset, f"{cname}.{f}"
