@@ -202,7 +202,8 @@ typedef struct prrtc_query {
 } prrtc_query;
 
 typedef struct prrtc_batch_settings {
-    prrtc_settings plan;             /* applied to every query (num_new_configs: see lanes) */
+    prrtc_settings plan;             /* applied to every query; a query gives up after
+                                        max_iters x num_new_configs samples, pRRTC's total */
     int lanes;                       /* virtual sampling lanes per query: sample k of a query is
                                         Halton point k / lanes + 1 of lane k % lanes, and the balance
                                         modes see the lane as pRRTC sees blockIdx.x.  0: 2.  pRRTC's

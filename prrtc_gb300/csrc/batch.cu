@@ -246,6 +246,9 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     P.cap = cap;
     P.path_pool_rows = b->path_rows;
     P.edge_order = settings->edge_order ? 1 : 0;
+    // pRRTC stops a query when any of its num_new_configs lanes passes max_iters
+    // (pRRTC.cu:343-346), i.e. after about max_iters x num_new_configs samples
+    P.max_samples_drawn = std::min<long long>((long long)S.max_iters * S.num_new_configs, 0x7fffffffLL);
     P.cfg_pool = reinterpret_cast<const float *>(base + o_cfg);
     P.queries = reinterpret_cast<const BatchQueryDesc *>(base + o_desc);
     P.slots = reinterpret_cast<SlotState *>(base + o_slots);

@@ -116,6 +116,7 @@ struct BatchParams {
     unsigned long long budget_ns;
     int num_queries, num_slots, cap, path_pool_rows;
     int edge_order;      // 0 contiguous, 1 interleaved (see warp_validate)
+    long long max_samples_drawn;   // per query: max_iters x num_new_configs, pRRTC's total budget
     const float *cfg_pool;
     const BatchQueryDesc *queries;
     SlotState *slots;

@@ -687,7 +687,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
         k = __shfl_sync(FULL, k, 0);
         const int vl = k % P.lanes;
         const int iter = k / P.lanes + 1;
-        if (iter > P.max_iters) {
+        if ((long long)k >= P.max_samples_drawn) {
             if (lane == 0) batch_finish(P, S, q, 0);
         } else {
             int t = 0;
