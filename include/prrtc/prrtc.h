@@ -214,6 +214,16 @@ typedef struct prrtc_batch_settings {
     int warps_per_block;             /* 0: 4 */
     int edge_order;                  /* order a warp checks an edge's points in: 0 contiguous
                                         rounds, 1 interleaved (every round spans the edge) */
+    int sampler;                     /* 0: pRRTC's Halton lanes; 1: Halton with per-query digit
+                                        scrambling and rotation (decorrelates large bases) */
+    int max_attempts;                /* independent attempts per query (0: 64; 1: none).  An attempt
+                                        that runs out of samples or arena restarts the query; once
+                                        no query is pending, idle warps open extra attempts of
+                                        queries running longer than k x restart_after_ns; the first
+                                        attempt to connect wins */
+    uint64_t restart_after_ns;       /* 0: 10 ms */
+    int max_workers_per_attempt;     /* warps working one attempt at once (0: unlimited); when every
+                                        running attempt is full, an idle warp opens a new attempt */
     int blocks_per_sm;               /* 0: occupancy maximum */
     int use_graph;                   /* replay each run as a captured CUDA graph */
     float margin;                    /* sphere inflation while planning, metres (>= 0) */
@@ -230,6 +240,7 @@ typedef struct prrtc_batch_stats {
     int blocks, warps_per_block;     /* launch shape used */
     int slots;                       /* resident query slots */
     int error;                       /* nonzero: a worker gave up waiting for work */
+    int extra_attempts;              /* attempts opened beyond each query's first */
     uint64_t configs_checked;        /* configurations validated (edge points examined) */
     uint64_t flops;                  /* algorithmic FLOPs of those checks: forward kinematics
                                         2 (12 dof + 9 spheres) per config, plus the primitive

@@ -79,7 +79,9 @@ class BatchSettings(C.Structure):
     """prrtc_batch_settings: planner settings for every query plus the batch's
     arena, launch shape, CUDA-graph and margin options."""
     _fields_ = [("plan", Settings), ("lanes", C.c_int), ("max_nodes_per_tree", C.c_int), ("max_active", C.c_int),
-                ("warps_per_block", C.c_int), ("edge_order", C.c_int), ("blocks_per_sm", C.c_int),
+                ("warps_per_block", C.c_int), ("edge_order", C.c_int), ("sampler", C.c_int),
+                ("max_attempts", C.c_int), ("restart_after_ns", C.c_uint64), ("max_workers_per_attempt", C.c_int),
+                ("blocks_per_sm", C.c_int),
                 ("use_graph", C.c_int),
                 ("margin", C.c_float), ("time_budget_ns", C.c_uint64)]
 
@@ -93,7 +95,7 @@ class BatchSettings(C.Structure):
 
 class _BatchStats(C.Structure):
     _fields_ = [("kernel_ns", C.c_uint64), ("samples", C.c_int64), ("solved", C.c_int), ("blocks", C.c_int),
-                ("warps_per_block", C.c_int), ("slots", C.c_int), ("error", C.c_int),
+                ("warps_per_block", C.c_int), ("slots", C.c_int), ("error", C.c_int), ("extra_attempts", C.c_int),
                 ("configs_checked", C.c_uint64), ("flops", C.c_uint64), ("nn_nodes", C.c_uint64)]
 
 

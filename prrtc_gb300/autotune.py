@@ -8,6 +8,10 @@ Sweeps, on a calibration batch of seeded queries, the knobs of
                        iteration round of a query);
 * ``edge_order``       edge tile shape: contiguous 32-point rounds or rounds
                        interleaved across the whole edge;
+* ``sampler``          the reference's Halton lanes or per-query scrambled
+                       Halton;
+* ``max_workers_per_attempt``  warps per attempt before idle warps open
+                       independent attempts (the tail's portfolio);
 
 and keeps the setting with the highest solved queries per second.  Results
 are cached in ``tuning.json`` next to this file, keyed by robot and workload:
@@ -22,8 +26,10 @@ import sys
 from pathlib import Path
 
 TUNING = Path(__file__).resolve().parent / "tuning.json"
-DEFAULT = {"lanes": 2, "warps_per_block": 4, "edge_order": 1}
-SPACE = {"lanes": (1, 2, 4), "warps_per_block": (2, 4), "edge_order": (0, 1)}
+DEFAULT = {"lanes": 2, "warps_per_block": 2, "edge_order": 0, "sampler": 1, "max_workers_per_attempt": 32}
+SPACE = {"lanes": (1, 2, 4), "warps_per_block": (2,), "edge_order": (0,), "sampler": (0, 1),
+         "max_workers_per_attempt": (16, 32, 64)}
+KNOBS = tuple(SPACE)
 
 
 def load(robot: str, workload: str | None = None) -> dict:
@@ -38,25 +44,31 @@ def load(robot: str, workload: str | None = None) -> dict:
     return dict(DEFAULT)
 
 
-def tune(ctx, robot, queries, plan, margin=1e-5, reps=2, space=None) -> dict:
+def tune(ctx, robot, queries, plan, margin=1e-5, reps=3, space=None) -> dict:
+    """Run every setting `reps` times and keep the one with the best median
+    batch time among those that solve the most queries."""
+    import statistics
     from .api import BatchSettings
     space = space or SPACE
     rows = []
-    for lanes, wpb, order in itertools.product(space["lanes"], space["warps_per_block"], space["edge_order"]):
-        bs = BatchSettings(plan, lanes=lanes, warps_per_block=wpb, edge_order=order, use_graph=1, margin=margin)
+    for values in itertools.product(*(space[k] for k in KNOBS)):
+        knobs = dict(zip(KNOBS, values))
+        bs = BatchSettings(plan, use_graph=1, margin=margin, **knobs)
         b = ctx.batch(robot, queries, bs)
         b.run()
-        ns, solved = 0, 0
+        times, solved = [], []
         for _ in range(reps):
             b.run()
             res = b.results()
-            ns += b.stats()["kernel_ns"]
-            solved += sum(r.solved for r in res)
+            times.append(b.stats()["kernel_ns"] * 1e-6)
+            solved.append(sum(r.solved for r in res))
         b.free()
-        rows.append({"lanes": lanes, "warps_per_block": wpb, "edge_order": order,
-                     "queries_per_s": solved / (ns * 1e-9), "ms_per_batch": ns / reps / 1e6})
-    best = max(rows, key=lambda r: r["queries_per_s"])
-    return {"best": {k: best[k] for k in ("lanes", "warps_per_block", "edge_order")}, "sweep": rows}
+        med = statistics.median(times)
+        rows.append({**knobs, "ms_median": med, "ms_all": times, "solved": min(solved),
+                     "queries_per_s": min(solved) / (med * 1e-3)})
+    top = max(r["solved"] for r in rows)
+    best = max((r for r in rows if r["solved"] == top), key=lambda r: r["queries_per_s"])
+    return {"best": {k: best[k] for k in KNOBS}, "sweep": rows}
 
 
 def main(argv):

@@ -23,8 +23,6 @@ struct Arena {
     float *nodes = nullptr;
     int *parents = nullptr;
     float *radii = nullptr;
-    int *tsel = nullptr;
-    int tsel_lanes = 0;
     bool in_use = false;
 };
 
@@ -34,7 +32,6 @@ static void arena_free(Arena *a)
     cudaFree(a->nodes);
     cudaFree(a->parents);
     cudaFree(a->radii);
-    cudaFree(a->tsel);
     delete a;
 }
 
@@ -45,10 +42,10 @@ void release_arena(Ctx *c)
 }
 
 // An arena of at least (slots, cap) for dof, NaN-filled; reuses the context's.
-static prrtc_status take_arena(Ctx *c, int dof, int cap, int slots, int lanes, Arena **out)
+static prrtc_status take_arena(Ctx *c, int dof, int cap, int slots, Arena **out)
 {
     Arena *a = c->arena;
-    if (a && !a->in_use && a->dof == dof && a->cap == cap && a->slots >= slots && a->tsel_lanes >= lanes) {
+    if (a && !a->in_use && a->dof == dof && a->cap == cap && a->slots >= slots) {
         a->in_use = true;
         *out = a;
         return PRRTC_OK;
@@ -61,11 +58,9 @@ static prrtc_status take_arena(Ctx *c, int dof, int cap, int slots, int lanes, A
     a->dof = dof;
     a->cap = cap;
     a->slots = slots;
-    a->tsel_lanes = std::max(lanes, 1);
     const size_t nn = (size_t)slots * 2 * dof * cap, np = (size_t)slots * 2 * cap;
     if (cudaMalloc(&a->nodes, nn * sizeof(float)) != cudaSuccess || cudaMalloc(&a->parents, np * sizeof(int)) != cudaSuccess ||
-        cudaMalloc(&a->radii, np * sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&a->tsel, (size_t)slots * a->tsel_lanes * sizeof(int)) != cudaSuccess) {
+        cudaMalloc(&a->radii, np * sizeof(float)) != cudaSuccess) {
         cudaGetLastError();
         arena_free(a);
         return c->fail(PRRTC_ENOMEM, "batch: cannot allocate an arena of %d slots x %d nodes", slots, cap);
@@ -185,7 +180,9 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     b->wpb = settings->warps_per_block > 0 ? settings->warps_per_block : 4;
     const size_t slot_bytes = (size_t)2 * cap * (D + 2) * sizeof(float);
     const size_t arena_budget = (size_t)16 << 30;
+    const int max_attempts = settings->max_attempts > 0 ? settings->max_attempts : 64;
     int slots = settings->max_active > 0 ? std::min(settings->max_active, n) : n;
+    if (max_attempts > 1) slots += std::max(64, n / 4);   // room for extra attempts in the tail
     slots = (int)std::max<size_t>(1, std::min<size_t>(slots, arena_budget / slot_bytes));
     b->slots = slots;
     b->path_rows = std::max(4096, n * 512);
@@ -199,6 +196,8 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     off = align256(off + std::max<size_t>(1, envs.size()) * sizeof(float4));
     const size_t o_desc = off;
     off = align256(off + n * sizeof(BatchQueryDesc));
+    const size_t o_qstate = off;
+    off = align256(off + n * sizeof(QueryState));
     const size_t o_slots = off;
     off = align256(off + slots * sizeof(SlotState));
     const size_t o_out = off;
@@ -217,11 +216,11 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     float4 *env_dev = reinterpret_cast<float4 *>(base + o_env);
     for (int i = 0; i < n; i++)
         if (env_rec_off[i] >= 0) descs[i].env = env_dev + env_rec_off[i];
-    if ((s = ensure_halton_bases(c, b->lanes)) ||
+    if ((s = ensure_halton_bases(c, b->lanes * max_attempts)) ||
         (s = c->cuda(cudaMemcpyAsync(base + o_cfg, cfg.data(), cfg.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream), "batch upload")) ||
         (!envs.empty() && (s = c->cuda(cudaMemcpyAsync(env_dev, envs.data(), envs.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream), "batch upload"))) ||
         (s = c->cuda(cudaMemcpyAsync(base + o_desc, descs.data(), n * sizeof(BatchQueryDesc), cudaMemcpyHostToDevice, c->stream), "batch upload")) ||
-        (s = take_arena(c, D, cap, slots, b->lanes, &b->arena)) ||
+        (s = take_arena(c, D, cap, slots, &b->arena)) ||
         (s = c->cuda(cudaEventCreate(&b->ev0), "event")) || (s = c->cuda(cudaEventCreate(&b->ev1), "event")) ||
         (s = c->cuda(cudaStreamSynchronize(c->stream), "batch upload"))) {
         prrtc_batch_free(ctx, b);
@@ -246,18 +245,23 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     P.cap = cap;
     P.path_pool_rows = b->path_rows;
     P.edge_order = settings->edge_order ? 1 : 0;
+    P.sampler = settings->sampler ? 1 : 0;
+    P.max_attempts = max_attempts;
+    P.max_workers = settings->max_workers_per_attempt > 0 ? settings->max_workers_per_attempt : 1 << 30;
+    P.bases_lanes = c->bases_lanes;
+    P.restart_after_ns = settings->restart_after_ns ? settings->restart_after_ns : 10000000ull;
     // pRRTC stops a query when any of its num_new_configs lanes passes max_iters
     // (pRRTC.cu:343-346), i.e. after about max_iters x num_new_configs samples
     P.max_samples_drawn = std::min<long long>((long long)S.max_iters * S.num_new_configs, 0x7fffffffLL);
     P.cfg_pool = reinterpret_cast<const float *>(base + o_cfg);
     P.queries = reinterpret_cast<const BatchQueryDesc *>(base + o_desc);
+    P.qstate = reinterpret_cast<QueryState *>(base + o_qstate);
     P.slots = reinterpret_cast<SlotState *>(base + o_slots);
     P.out = reinterpret_cast<BatchOut *>(base + o_out);
     P.ctr = reinterpret_cast<BatchCounters *>(base + o_ctr);
     P.nodes = b->arena->nodes;
     P.parents = b->arena->parents;
     P.radii = b->arena->radii;
-    P.tsel = b->arena->tsel;
     P.path_pool = reinterpret_cast<float *>(base + o_path);
     P.halton_bases = c->bases;
     prrtc_robot_limits(robot, P.scale, P.offset);
@@ -277,6 +281,7 @@ static prrtc_status enqueue_run(Ctx *c, prrtc_batch *b, const RobotOps *ops)
 {
     prrtc_status s;
     if ((s = c->cuda(cudaMemsetAsync(b->P.slots, 0, b->slots * sizeof(SlotState), c->stream), "batch reset")) ||
+        (s = c->cuda(cudaMemsetAsync(b->P.qstate, 0, b->n * sizeof(QueryState), c->stream), "batch reset")) ||
         (s = c->cuda(cudaMemsetAsync(b->P.out, 0, b->n * sizeof(BatchOut), c->stream), "batch reset")) ||
         (s = c->cuda(cudaMemsetAsync(b->P.ctr, 0, sizeof(BatchCounters), c->stream), "batch reset")) ||
         (s = c->cuda(ops->solve_batch(b->P, b->blocks, b->wpb, c->stream), "batch launch")))
@@ -320,6 +325,7 @@ extern "C" prrtc_status prrtc_batch_run(prrtc_ctx *ctx, prrtc_batch *b)
     b->stats.kernel_ns = (uint64_t)(ms * 1e6);
     b->stats.error = ctr.error;
     b->stats.configs_checked = ctr.work[1];
+    b->stats.extra_attempts = ctr.attempts;
     b->stats.flops = ctr.work[0];
     b->stats.nn_nodes = ctr.nn_nodes;
     b->ran = true;

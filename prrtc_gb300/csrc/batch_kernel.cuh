@@ -1,0 +1,663 @@
+// Batched form of the planner: many queries, one persistent launch.
+//
+// Every warp is an independent worker.  A slot holds one *attempt* at a query:
+// its own pair of trees in the arena and its own sample stream.  A worker
+// joins a running slot and runs RRT-Connect iterations there until the slot
+// ends, then moves to the next running slot (round-robin cursor), so the warps
+// of finished queries are stolen by unfinished ones.  The last warp to leave
+// an ended slot scrubs its arena region back to NaN and reuses the slot:
+// restarting the query (if its only attempt ran out of samples or arena) or
+// admitting the next pending query.  When no query is pending, idle warps open
+// extra attempts of long-running queries in free slots: RRT-Connect's run
+// time is heavy-tailed in narrow passages, and the first of several
+// independent attempts to connect ends the query (the others are cancelled).
+//
+// Sampling follows the reference's lanes virtually: sample k of an attempt is
+// Halton point k / L + 1 of virtual lane k % L (pRRTC.cu:81-105), with that
+// lane's prime bases (sampler 0: the reference's per-block shuffled bases,
+// offset by L lanes per attempt) or per-(query, attempt) digit-scrambled bases
+// (sampler 1).  The balance modes see the virtual lane as pRRTC sees
+// blockIdx.x.
+#pragma once
+
+#include "device_common.cuh"
+#include "planner_device.cuh"
+#include "prrtc_internal.h"
+
+namespace prrtc {
+
+struct WarpScratch {
+    float from[16], step[16], cfg[16], nn[16], vec[16], next[16];
+    int bad;
+    int pad_[3];
+};
+
+// Whole warp: check the g points of the edge in W (from + k * step),
+// k = 1..g, in ceil(g / 32) rounds of one point per lane.  Contiguous order
+// gives round r the points 32 r + lane + 1; interleaved order gives it
+// lane * R + r + 1, so the first round already samples the whole edge at
+// stride R.  Adds the work done to work[0] (FLOPs) and work[1] (points).
+template <class Gen>
+__device__ __forceinline__ bool warp_validate(const WarpScratch &W, int g, int interleave, CheckCtx &ctx,
+                                              unsigned long long *work)
+{
+    constexpr int D = Gen::kDof;
+    const int lane = lane_id();
+    volatile int *flag = ctx.stop_flag;
+    if (lane == 0) *flag = 0;
+    __syncwarp();
+    bool bad = false;
+    int n = 0;
+    unsigned long long flops = 0;
+    const int R = (g + 31) >> 5;
+    for (int r = 0; r < R; r++) {
+        const int k = interleave ? lane * R + r + 1 : 32 * r + lane + 1;
+        const bool run = k <= g && !*flag;
+        if (run) {
+            float q[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) q[d] = __fadd_rn(W.from[d], __fmul_rn((float)k, W.step[d]));
+            ctx.work = 0;
+            if (!Gen::fkcc(q, ctx)) {
+                bad = true;
+                *flag = 1;
+            }
+            flops += ctx.work + Gen::kFkFlops;
+        }
+        n += __popc(__ballot_sync(0xffffffffu, run));
+        if (__any_sync(0xffffffffu, bad)) break;
+    }
+    flops = warp_sum(flops);
+    if (lane == 0) {
+        atomicAdd(work, flops);
+        atomicAdd(work + 1, (unsigned long long)n);
+    }
+    return !__any_sync(0xffffffffu, bad);
+}
+
+__device__ __forceinline__ int vload(const int *p) { return *(const volatile int *)p; }
+
+// lane 0: publish an unsolved query's result (first caller wins)
+__device__ __forceinline__ void finish_query_unsolved(const BatchParams &P, const SlotState *S, int q, int status)
+{
+    if (atomicCAS(&P.qstate[q].state, 1, 2) != 1) return;
+    BatchOut &o = P.out[q];
+    const volatile SlotState *vs = S;
+    o.solved = 0;
+    o.status = status;
+    o.start_tree_size = min(vs->free_index[0], P.cap);
+    o.goal_tree_size = min(vs->free_index[1], P.cap);
+    o.path_length = 0;
+    o.iters = -1;
+    o.cost = 0.0f;
+    o.path_rows = 0;
+    o.samples = vs->ticket;
+    o.t_done = global_ns();
+    __threadfence();
+    atomicAdd(&P.ctr->done, 1);
+}
+
+// lane 0: end the attempt in slot S unsolved (first caller wins).  The last
+// live attempt of a query either asks for a restart in this slot or, when the
+// query has used its attempts (or on timeout), publishes it as unsolved.
+__device__ __forceinline__ void finish_attempt(const BatchParams &P, SlotState *S, int q, int status)
+{
+    if (atomicCAS(&S->state, SLOT_RUNNING, SLOT_DONE) != SLOT_RUNNING) return;
+    const int live = atomicSub(&P.qstate[q].live, 1) - 1;
+    if (status == PRRTC_ETIMEDOUT) {
+        finish_query_unsolved(P, S, q, status);
+        return;
+    }
+    if (live == 0 && vload(&P.qstate[q].state) == 1) {
+        if (vload(&P.qstate[q].attempts) < P.max_attempts)
+            S->restart = 1;
+        else
+            finish_query_unsolved(P, S, q, status);
+    }
+}
+
+// lane 0: walk a tree from `start` to its root; returns the node count
+// (root excluded) or -1 on a broken chain.
+template <int D>
+__device__ int chain_length(const int *parents, int cap, int start, int *root)
+{
+    const volatile int *vp = parents;
+    int cur = start;
+    for (int n = 0; n <= cap; n++) {
+        const int par = vp[cur];
+        if (par == cur) {
+            *root = cur;
+            return n;
+        }
+        if (par < 0 || par >= cap) return -1;
+        cur = par;
+    }
+    return -1;
+}
+
+// lane 0, after winning the query: trace the solution into the path pool in
+// the reference's order (goal, goal-tree segment toward the junction,
+// start-tree segment, start; pRRTC.cu:731-741) and publish the result.
+template <int D>
+__device__ void batch_trace(const BatchParams &P, const SlotState *S, int s, int q, int t, int jt, int jo, int iter)
+{
+    const float *nodes_s = P.nodes + (size_t)s * 2 * D * P.cap;
+    const int *par_s = P.parents + (size_t)s * 2 * P.cap;
+    const int o = 1 - t;
+    const int j0 = t == 0 ? jt : jo, j1 = t == 0 ? jo : jt;
+    int r0 = 0, r1 = 0;
+    const int n0 = chain_length<D>(par_s, P.cap, j0, &r0);
+    const int n1 = chain_length<D>(par_s + P.cap, P.cap, j1, &r1);
+    BatchOut &out = P.out[q];
+    const volatile SlotState *vs = S;
+    out.solved = 1;
+    out.iters = iter;
+    out.reached_goal = r1;
+    out.start_tree_size = min(vs->free_index[0], P.cap);
+    out.goal_tree_size = min(vs->free_index[1], P.cap);
+    out.samples = vs->ticket;
+    out.path_rows = 0;
+    out.status = PRRTC_ENOMEM;
+    if (n0 >= 0 && n1 >= 0) {
+        const int rows = n0 + n1 + 2;
+        const int off = atomicAdd(&P.ctr->path_next, rows);
+        const bool fits = off + rows <= P.path_pool_rows;
+        // cost in the reference's order: the connecting tree first, then the other
+        float cost = 0.0f;
+        for (int pass = 0; pass < 2; pass++) {
+            const int tree = pass == 0 ? t : o;
+            const float *nd = nodes_s + (size_t)tree * D * P.cap;
+            const int *pr = par_s + (size_t)tree * P.cap;
+            int cur = tree == 0 ? j0 : j1;
+            const int n = tree == 0 ? n0 : n1;
+            for (int i = 0; i < n; i++) {
+                const int par = vload(pr + cur);
+                float acc = 0.0f;
+                const int row = tree == 0 ? off + n1 + 1 + i : off + n1 - i;
+#pragma unroll
+                for (int d = 0; d < D; d++) {
+                    const float a = __ldcg(nd + (size_t)d * P.cap + cur);
+                    const float b = __ldcg(nd + (size_t)d * P.cap + par);
+                    const float df = a - b;
+                    acc = fmaf(df, df, acc);
+                    if (fits) P.path_pool[(size_t)row * D + d] = a;
+                }
+                cost += sqrtf(acc);
+                cur = par;
+            }
+        }
+        out.cost = cost;
+        out.path_length = n0 + n1;
+        if (fits) {
+            const BatchQueryDesc &Q = P.queries[q];
+            const float *start = P.cfg_pool + Q.cfg_off;
+            const float *goal = start + D + (size_t)r1 * D;
+#pragma unroll
+            for (int d = 0; d < D; d++) {
+                P.path_pool[(size_t)off * D + d] = goal[d];
+                P.path_pool[(size_t)(off + rows - 1) * D + d] = start[d];
+            }
+            out.path_off = off;
+            out.path_rows = rows;
+            out.status = 0;
+        }
+    }
+    out.t_done = global_ns();
+    __threadfence();
+    atomicAdd(&P.ctr->done, 1);
+}
+
+// whole warp: write query qa's roots into slot s as attempt `attempt` and start it
+template <int D>
+__device__ void batch_admit(const BatchParams &P, int s, int qa, int attempt)
+{
+    const int lane = lane_id();
+    const BatchQueryDesc Q = P.queries[qa];
+    float *nodes_s = P.nodes + (size_t)s * 2 * D * P.cap;
+    int *par_s = P.parents + (size_t)s * 2 * P.cap;
+    float *rad_s = P.radii + (size_t)s * 2 * P.cap;
+    const float *cfg = P.cfg_pool + Q.cfg_off;
+    if (lane < D) nodes_s[(size_t)lane * P.cap] = cfg[lane];
+    for (int i = lane; i < Q.num_goals * D; i += 32) {
+        const int g = i / D, d = i % D;
+        nodes_s[(size_t)D * P.cap + (size_t)d * P.cap + g] = cfg[D + i];
+    }
+    for (int g = lane; g < Q.num_goals; g += 32) {
+        par_s[P.cap + g] = g;
+        rad_s[P.cap + g] = FLT_MAX;
+    }
+    if (lane == 0) {
+        par_s[0] = 0;
+        rad_s[0] = FLT_MAX;
+        SlotState *S = &P.slots[s];
+        S->query = qa;
+        S->attempt = attempt;
+        S->restart = 0;
+        S->free_index[0] = 1;
+        S->free_index[1] = Q.num_goals;
+        S->ticket = 0;
+    }
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) atomicExch(&P.slots[s].state, SLOT_RUNNING);
+}
+
+// lane 0: a new query's first attempt
+__device__ __forceinline__ void open_query(const BatchParams &P, int qa)
+{
+    QueryState &qs = P.qstate[qa];
+    qs.attempts = 1;
+    qs.live = 1;
+    qs.t_first = global_ns();
+    P.out[qa].t_admit = qs.t_first;
+    __threadfence();
+    atomicExch(&qs.state, 1);
+}
+
+// whole warp: restore slot s's used arena prefix to NaN
+template <int D>
+__device__ void batch_scrub(const BatchParams &P, int s)
+{
+    const volatile SlotState *vs = &P.slots[s];
+    float *nodes_s = P.nodes + (size_t)s * 2 * D * P.cap;
+    for (int t = 0; t < 2; t++) {
+        const int n = min(vs->free_index[t], P.cap);
+        float *nd = nodes_s + (size_t)t * D * P.cap;
+        for (int d = 0; d < D; d++)
+            for (int i = lane_id(); i < n; i += 32) nd[(size_t)d * P.cap + i] = __int_as_float(0xFFFFFFFF);
+    }
+    __threadfence();
+    __syncwarp();
+}
+
+// whole warp: leave slot s.  The last warp out of an ended slot scrubs it and
+// reuses it: a restart of its query if one was asked for, else the next
+// pending query.  Returns true when this warp now works on the reused slot.
+template <int D>
+__device__ bool batch_leave(const BatchParams &P, int s, bool allow_admit)
+{
+    const int lane = lane_id();
+    int recycle = 0;
+    if (lane == 0) {
+        __threadfence();
+        SlotState *S = &P.slots[s];
+        const int left = atomicSub(&S->workers, 1) - 1;
+        recycle = left == 0 && atomicCAS(&S->state, SLOT_DONE, SLOT_BUSY) == SLOT_DONE;
+    }
+    recycle = __shfl_sync(0xffffffffu, recycle, 0);
+    if (!recycle) return false;
+    batch_scrub<D>(P, s);
+    int qa = -1, att = 0;
+    if (lane == 0 && allow_admit) {
+        SlotState *S = &P.slots[s];
+        const int q = S->query;
+        if (S->restart && vload(&P.qstate[q].state) == 1) {
+            att = atomicAdd(&P.qstate[q].attempts, 1);
+            if (att < P.max_attempts) {
+                atomicAdd(&P.qstate[q].live, 1);
+                atomicAdd(&P.ctr->attempts, 1);
+                qa = q;
+            } else if (vload(&P.qstate[q].live) == 0) {
+                finish_query_unsolved(P, S, q, 0);
+            }
+        }
+        if (qa < 0 && vload(&P.ctr->admit_next) < P.num_queries) {
+            qa = atomicAdd(&P.ctr->admit_next, 1);
+            if (qa >= P.num_queries) {
+                qa = -1;
+            } else {
+                att = 0;
+                open_query(P, qa);
+            }
+        }
+        if (qa >= 0) atomicAdd(&S->workers, 1);
+    }
+    qa = __shfl_sync(0xffffffffu, qa, 0);
+    att = __shfl_sync(0xffffffffu, att, 0);
+    if (qa >= 0) {
+        batch_admit<D>(P, s, qa, att);
+        return true;
+    }
+    if (lane == 0) atomicExch(&P.slots[s].state, SLOT_FREE);
+    return false;
+}
+
+// whole warp: a running query that may get one more attempt, scanning from
+// `from`; -1 if none.  A query qualifies after running k x restart_after_ns
+// with k attempts, or at once when `forced` (every running attempt is at its
+// worker cap, so an idle warp would otherwise wait).
+__device__ __forceinline__ int spawn_candidate(const BatchParams &P, unsigned from, unsigned long long now,
+                                               bool forced)
+{
+    for (int base = 0; base < P.num_queries; base += 32) {
+        const int q = (int)((from + (unsigned)base + (unsigned)lane_id()) % (unsigned)P.num_queries);
+        bool ok = false;
+        if (base + lane_id() < P.num_queries) {
+            const QueryState &qs = P.qstate[q];
+            const int a = vload(&qs.attempts);
+            ok = vload(&qs.state) == 1 && a < P.max_attempts &&
+                 (forced ||
+                  now - *(const volatile unsigned long long *)&qs.t_first > P.restart_after_ns * (unsigned long long)a);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, ok);
+        if (m) return __shfl_sync(0xffffffffu, q, __ffs(m) - 1);
+    }
+    return -1;
+}
+
+template <class Gen>
+__global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
+{
+    constexpr int D = Gen::kDof;
+    constexpr unsigned FULL = 0xffffffffu;
+    extern __shared__ float4 s_raw[];
+    WarpScratch &W = reinterpret_cast<WarpScratch *>(s_raw)[threadIdx.x >> 5];
+    const int lane = lane_id();
+    BatchCounters *C = P.ctr;
+    const float fg = (float)P.granularity;
+    if (lane == 0) atomicCAS(&C->t0, 0ull, global_ns());
+    int slot = -1;
+    unsigned idle = 0;
+
+    while (true) {
+        // ---- time budget
+        int timed_out = 0;
+        if (lane == 0 && P.budget_ns) timed_out = global_ns() - *(volatile unsigned long long *)&C->t0 > P.budget_ns;
+        timed_out = __shfl_sync(FULL, timed_out, 0);
+        if (timed_out) {
+            if (slot >= 0) {
+                if (lane == 0) finish_attempt(P, &P.slots[slot], P.slots[slot].query, PRRTC_ETIMEDOUT);
+                __syncwarp();
+                batch_leave<D>(P, slot, false);
+            }
+            return;
+        }
+        // ---- find work: a pending query, else a running attempt with room for
+        // another warp; in the tail, free slots become extra attempts
+        if (slot < 0) {
+            int found = -1, admit = -1, rec = -1, free_slot = -1, joinable = 0;
+            unsigned s0 = 0;
+            if (lane == 0) {
+                s0 = atomicAdd((unsigned *)&C->cursor, 1u);
+                const bool pending = vload(&C->admit_next) < P.num_queries;
+                for (int tries = 0; tries < P.num_slots; tries++) {
+                    const int s = (int)((s0 + (unsigned)tries) % (unsigned)P.num_slots);
+                    SlotState *S = &P.slots[s];
+                    const int st = vload(&S->state);
+                    if (st == SLOT_FREE && pending) {
+                        if (atomicCAS(&S->state, SLOT_FREE, SLOT_BUSY) != SLOT_FREE) continue;
+                        const int qa = atomicAdd(&C->admit_next, 1);
+                        if (qa < P.num_queries) {
+                            open_query(P, qa);
+                            atomicAdd(&S->workers, 1);
+                            found = s;
+                            admit = qa;
+                            break;
+                        }
+                        atomicExch(&S->state, SLOT_FREE);
+                    } else if (st == SLOT_FREE && free_slot < 0 && P.max_attempts > 1) {
+                        if (atomicCAS(&S->state, SLOT_FREE, SLOT_BUSY) == SLOT_FREE) free_slot = s;
+                    } else if (st == SLOT_RUNNING) {
+                        if (vload(&S->workers) >= P.max_workers) continue;
+                        joinable = 1;
+                        atomicAdd(&S->workers, 1);
+                        if (vload(&S->state) == SLOT_RUNNING)
+                            found = s;
+                        else
+                            rec = s;        // leave it again (possibly recycling it)
+                        break;
+                    }
+                }
+                if (free_slot >= 0 && (found >= 0 || rec >= 0)) {
+                    atomicExch(&P.slots[free_slot].state, SLOT_FREE);
+                    free_slot = -1;
+                }
+            }
+            found = __shfl_sync(FULL, found, 0);
+            admit = __shfl_sync(FULL, admit, 0);
+            rec = __shfl_sync(FULL, rec, 0);
+            free_slot = __shfl_sync(FULL, free_slot, 0);
+            joinable = __shfl_sync(FULL, joinable, 0);
+            s0 = __shfl_sync(FULL, s0, 0);
+            if (free_slot >= 0) {
+                // nothing to join: an extra attempt of a running query
+                const int qc = spawn_candidate(P, s0 * 7919u, global_ns(), !joinable);
+                int att = -1;
+                if (lane == 0) {
+                    if (qc >= 0) {
+                        att = atomicAdd(&P.qstate[qc].attempts, 1);
+                        if (att < P.max_attempts && vload(&P.qstate[qc].state) == 1) {
+                            atomicAdd(&P.qstate[qc].live, 1);
+                            atomicAdd(&C->attempts, 1);
+                            atomicAdd(&P.slots[free_slot].workers, 1);
+                        } else {
+                            att = -1;
+                        }
+                    }
+                    if (att < 0) atomicExch(&P.slots[free_slot].state, SLOT_FREE);
+                }
+                att = __shfl_sync(FULL, att, 0);
+                if (att >= 0) {
+                    batch_admit<D>(P, free_slot, qc, att);
+                    slot = free_slot;
+                    idle = 0;
+                    continue;
+                }
+            }
+            if (rec >= 0) {
+                if (batch_leave<D>(P, rec, true)) {
+                    slot = rec;
+                    idle = 0;
+                }
+                continue;
+            }
+            if (found < 0) {
+                int all_done = 0;
+                if (lane == 0) all_done = vload(&C->done) >= P.num_queries;
+                if (__shfl_sync(FULL, all_done, 0)) return;
+                if (++idle > (1u << 22)) {
+                    if (lane == 0) atomicOr(&C->error, 1);
+                    return;
+                }
+                __nanosleep(256);
+                continue;
+            }
+            if (admit >= 0) batch_admit<D>(P, found, admit, 0);
+            slot = found;
+            idle = 0;
+        }
+
+        // ---- one RRT-Connect iteration on `slot`
+        SlotState *S = &P.slots[slot];
+        const int q = vload(&S->query);
+        const int attempt = vload(&S->attempt);
+        const BatchQueryDesc Qd = P.queries[q];
+        CheckCtx ctx{{Qd.env, Qd.env_n}, P.pad, &W.bad};
+        float *nodes_s = P.nodes + (size_t)slot * 2 * D * P.cap;
+        int *par_s = P.parents + (size_t)slot * 2 * P.cap;
+        float *rad_s = P.radii + (size_t)slot * 2 * P.cap;
+
+        int k = 0, qdone = 0;
+        if (lane == 0) {
+            qdone = vload(&P.qstate[q].state) == 2;
+            if (qdone) {
+                // another attempt finished the query: cancel this one
+                if (atomicCAS(&S->state, SLOT_RUNNING, SLOT_DONE) == SLOT_RUNNING) atomicSub(&P.qstate[q].live, 1);
+            } else {
+                k = atomicAdd(&S->ticket, 1);
+            }
+        }
+        qdone = __shfl_sync(FULL, qdone, 0);
+        k = __shfl_sync(FULL, k, 0);
+        const int vl = k % P.lanes;
+        const int iter = k / P.lanes + 1;
+        if (qdone) {
+            // leave below
+        } else if ((long long)k >= P.max_samples_drawn) {
+            if (lane == 0) finish_attempt(P, S, q, 0);
+        } else {
+            int t = 0;
+            if (lane == 0) {
+                volatile SlotState *vs = S;
+                const int f0 = vs->free_index[0], f1 = vs->free_index[1];
+                const int L = P.lanes;
+                if (P.balance == 0 || iter == 1) {
+                    t = (vl < (L / 2)) ? 0 : 1;
+                } else if (P.balance == 1 && 2 * abs(f0 - f1) < 3 * L) {
+                    const float ratio = f0 / (float)(f0 + f1);
+                    t = ((float)vl < L * (1.0f - ratio)) ? 0 : 1;
+                } else if (P.balance == 1) {
+                    const float ratio = f0 / (float)(f0 + f1);
+                    t = ratio < P.tree_ratio ? 0 : 1;
+                } else {
+                    // vamp balance (pRRTC.cu:364-371): a lane swaps trees unless the
+                    // other is much larger.  The lane's previous tree is taken as
+                    // alternating from its first choice, so no per-lane state is
+                    // shared by the warps working on the attempt.
+                    const int prev = ((iter - 1) + (vl < (L / 2) ? 0 : 1)) & 1;
+                    const int ft = prev == 0 ? f0 : f1, fo = prev == 0 ? f1 : f0;
+                    const float ratio = abs(ft - fo) / (float)ft;
+                    t = ratio < P.tree_ratio ? 1 - prev : prev;
+                }
+            }
+            t = __shfl_sync(FULL, t, 0);
+            const int o = 1 - t;
+            float *nd_t = nodes_s + (size_t)t * D * P.cap, *nd_o = nodes_s + (size_t)o * D * P.cap;
+            int *pr_t = par_s + (size_t)t * P.cap;
+            float *rd_t = rad_s + (size_t)t * P.cap;
+            if (lane < D) {
+                float h;
+                if (P.sampler == 0) {
+                    const int row = (vl + attempt * P.lanes) % P.bases_lanes;
+                    h = radical_inverse((unsigned)iter, (unsigned)P.halton_bases[row * 16 + lane]);
+                } else {
+                    // scrambled Halton: digit multiplier and rotation per (query, attempt, dimension)
+                    const unsigned b = (unsigned)P.halton_bases[vl % P.bases_lanes * 16 + lane];
+                    const unsigned hs = hash32((unsigned)q * 0x9E3779B1u + (unsigned)attempt * 0xC2B2AE35u +
+                                               (unsigned)lane * 0x85EBCA77u + 0x165667B1u);
+                    h = scrambled_radical_inverse((unsigned)iter, b, 1u + hs % (b - 1u));
+                    h += (float)(hs >> 8) * (1.0f / 16777216.0f);
+                    h -= floorf(h);
+                }
+                W.cfg[lane] = fmaf(h, P.scale[lane], P.offset[lane]);
+            }
+            __syncwarp();
+            float qv[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) qv[d] = W.cfg[d];
+            float dsq;
+            int ni;
+            const int cnt_t = vload(&S->free_index[t]);
+            warp_nn<D>(nd_t, P.cap, cnt_t, qv, dsq, ni);
+            if (lane == 0) atomicAdd(&C->nn_nodes, (unsigned long long)min(cnt_t, P.cap));
+            const float dist = sqrtf(dsq);
+            const float scale = fminf(1.0f, P.range / dist);
+            int skip = 0;
+            if (lane == 0) skip = P.dynamic_domain && __ldcg(rd_t + ni) < dist;
+            skip = __shfl_sync(FULL, skip, 0);
+            if (!skip) {
+                if (lane < D) {
+                    const float nn = __ldcg(nd_t + (size_t)lane * P.cap + ni);
+                    const float c = fmaf(W.cfg[lane] - nn, scale, nn);
+                    W.nn[lane] = nn;
+                    W.from[lane] = nn;
+                    W.cfg[lane] = c;
+                    W.step[lane] = __fdiv_rn(__fsub_rn(c, nn), fg);
+                }
+                __syncwarp();
+                if (!warp_validate<Gen>(W, P.granularity, P.edge_order, ctx, C->work)) {
+                    if (lane == 0 && P.dynamic_domain) dd_shrink(rd_t + ni, P.dd_alpha, P.dd_radius, P.dd_min_radius);
+                } else {
+                    int idx = -1;
+                    if (lane == 0) {
+                        idx = atomicAdd(&S->free_index[t], 1);
+                        if (idx >= P.max_samples || idx >= P.cap) {
+                            finish_attempt(P, S, q, idx >= P.max_samples ? 0 : PRRTC_ENOMEM);
+                            idx = -1;
+                        } else {
+                            pr_t[idx] = ni;
+                            if (P.dynamic_domain) {
+                                rd_t[idx] = FLT_MAX;
+                                dd_grow(rd_t + ni, P.dd_alpha);
+                            }
+                        }
+                    }
+                    idx = __shfl_sync(FULL, idx, 0);
+                    if (idx >= 0) {
+                        if (lane < D) nd_t[(size_t)lane * P.cap + idx] = W.cfg[lane];
+                        __threadfence();
+                        __syncwarp();
+                        // connect toward the other tree (pRRTC.cu:478-551)
+#pragma unroll
+                        for (int d = 0; d < D; d++) qv[d] = W.cfg[d];
+                        int oi;
+                        const int cnt_o = vload(&S->free_index[o]);
+                        warp_nn<D>(nd_o, P.cap, cnt_o, qv, dsq, oi);
+                        if (lane == 0) atomicAdd(&C->nn_nodes, (unsigned long long)min(cnt_o, P.cap));
+                        const unsigned n_ext = (unsigned)ceilf(sqrtf(dsq) / P.range);
+                        if (lane < D) W.vec[lane] = (__ldcg(nd_o + (size_t)lane * P.cap + oi) - W.cfg[lane]) / (float)n_ext;
+                        __syncwarp();
+                        unsigned i_ext = 0;
+                        int parent = idx;
+                        while (i_ext < n_ext) {
+                            if (lane < D) {
+                                const float a = W.cfg[lane];
+                                const float b = a + W.vec[lane];
+                                W.next[lane] = b;
+                                W.from[lane] = a;
+                                W.step[lane] = __fdiv_rn(__fsub_rn(b, a), fg);
+                            }
+                            __syncwarp();
+                            if (!warp_validate<Gen>(W, P.granularity, P.edge_order, ctx, C->work)) break;
+                            int idx2 = -1;
+                            if (lane == 0) {
+                                idx2 = atomicAdd(&S->free_index[t], 1);
+                                if (idx2 >= P.max_samples || idx2 >= P.cap) {
+                                    finish_attempt(P, S, q, idx2 >= P.max_samples ? 0 : PRRTC_ENOMEM);
+                                    idx2 = -1;
+                                } else {
+                                    pr_t[idx2] = parent;
+                                    rd_t[idx2] = FLT_MAX;
+                                }
+                            }
+                            idx2 = __shfl_sync(FULL, idx2, 0);
+                            if (idx2 < 0) {
+                                parent = -1;
+                                break;
+                            }
+                            if (lane < D) {
+                                W.cfg[lane] = W.next[lane];
+                                nd_t[(size_t)lane * P.cap + idx2] = W.next[lane];
+                            }
+                            __threadfence();
+                            __syncwarp();
+                            parent = idx2;
+                            i_ext++;
+                        }
+                        if (i_ext == n_ext && parent >= 0 && lane == 0) {
+                            // connected: end the attempt, then the first attempt to
+                            // win the query traces the path
+                            if (atomicCAS(&S->state, SLOT_RUNNING, SLOT_DONE) == SLOT_RUNNING) {
+                                atomicSub(&P.qstate[q].live, 1);
+                                if (atomicCAS(&P.qstate[q].state, 1, 2) == 1) {
+                                    __threadfence();
+                                    batch_trace<D>(P, S, slot, q, t, parent, oi, iter);
+                                }
+                            }
+                        }
+                        __syncwarp();
+                    }
+                }
+            }
+        }
+        // ---- leave an ended slot
+        int st = 0;
+        if (lane == 0) st = vload(&S->state);
+        st = __shfl_sync(FULL, st, 0);
+        if (st != SLOT_RUNNING) {
+            if (!batch_leave<D>(P, slot, true)) slot = -1;
+        }
+    }
+}
+
+}  // namespace prrtc

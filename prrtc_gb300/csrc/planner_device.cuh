@@ -226,4 +226,30 @@ __device__ __forceinline__ float radical_inverse(unsigned i, unsigned b)
     return r;
 }
 
+// Radical inverse with every digit multiplied by a (mod b), a in [1, b-1]:
+// a linear digit scrambling that breaks the correlations between the
+// sequences of large prime bases while keeping each dimension's
+// low-discrepancy structure.
+__device__ __forceinline__ float scrambled_radical_inverse(unsigned i, unsigned b, unsigned a)
+{
+    const float inv = 1.0f / (float)b;
+    float f = inv, r = 0.0f;
+    while (i > 0) {
+        r = fmaf(f, (float)((a * (i % b)) % b), r);
+        i /= b;
+        f *= inv;
+    }
+    return r;
+}
+
+__device__ __forceinline__ unsigned hash32(unsigned x)
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
 }  // namespace prrtc

@@ -68,14 +68,25 @@ struct BatchQueryDesc {
 
 enum SlotStateCode { SLOT_FREE = 0, SLOT_RUNNING = 1, SLOT_DONE = 2, SLOT_BUSY = 3 };
 
-// One resident query slot (its trees live in the arena at the slot's index).
+// One resident slot: an attempt at a query (its trees live in the arena at
+// the slot's index).
 struct SlotState {
     int query;
+    int attempt;         // attempt number of the query (selects its sample stream)
     int state;           // SlotStateCode
     int free_index[2];
     int ticket;          // samples drawn so far
     int workers;         // warps registered on the slot
-    int pad_[2];
+    int restart;         // 1: the warp that recycles the slot restarts the query here
+};
+
+// Per-query state shared by its attempts.
+struct QueryState {
+    int state;           // 0 pending, 1 running, 2 finished
+    int attempts;        // attempts started
+    int live;            // attempts running
+    int pad_;
+    unsigned long long t_first;   // first admission, device ns
 };
 
 // Per-query result, written by the warp that finishes the query.
@@ -99,7 +110,8 @@ struct BatchCounters {
     int done;            // queries finished
     int path_next;       // rows used in the path pool
     int error;           // bit 0: a worker gave up waiting for work
-    int pad_[3];
+    int attempts;        // attempts started beyond each query's first
+    int pad_[2];
     unsigned long long t0;
     unsigned long long work[2];      // algorithmic FLOPs of the checks, configurations checked
     unsigned long long nn_nodes;     // tree nodes visited by nearest-neighbour scans
@@ -117,15 +129,20 @@ struct BatchParams {
     int num_queries, num_slots, cap, path_pool_rows;
     int edge_order;      // 0 contiguous, 1 interleaved (see warp_validate)
     long long max_samples_drawn;   // per query: max_iters x num_new_configs, pRRTC's total budget
+    int sampler;         // 0 Halton lanes as pRRTC, 1 scrambled Halton per query
+    int max_attempts;    // attempts per query (restarts and parallel attempts), >= 1
+    int max_workers;     // warps per attempt
+    int bases_lanes;     // rows of halton_bases
+    unsigned long long restart_after_ns;   // a query may get its k-th extra attempt after k x this
     const float *cfg_pool;
     const BatchQueryDesc *queries;
+    QueryState *qstate;
     SlotState *slots;
     BatchOut *out;
     BatchCounters *ctr;
     float *nodes;        // [slot][2][dof][cap], NaN where unwritten
     int *parents;        // [slot][2][cap]
     float *radii;        // [slot][2][cap]
-    int *tsel;           // [slot][lanes] balance-2 tree choice per virtual lane
     float *path_pool;    // [path_pool_rows][dof]
     const float *halton_bases;   // [lanes][16]
     float scale[16], offset[16];

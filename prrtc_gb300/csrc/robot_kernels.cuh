@@ -325,516 +325,11 @@ __global__ void __launch_bounds__(256) k_rrtc_plain(const PlainParams P)
     add_work(P.work, my_flops, my_cfgs);
 }
 
-// ---------------------------------------------------------------------------
-// Batched form: many queries, one persistent launch.  Every warp is an
-// independent worker.  Queries occupy slots (trees in a slot-indexed arena);
-// a worker joins a running slot, runs one RRT-Connect iteration there, and
-// keeps iterating until the slot's query is finished; then it moves on to the
-// next running slot (round-robin cursor), so the warps of finished queries are
-// stolen by the unfinished ones.  The last warp to leave a finished slot
-// restores its arena region to NaN and admits the next pending query into it.
-//
-// Sampling follows the reference's lanes virtually: sample k of a query is
-// Halton point k / L + 1 of virtual lane k % L, whose prime bases are that
-// lane's (the reference's per-block shuffled bases); balance modes use the
-// virtual lane as the reference uses blockIdx.
+}  // namespace prrtc
 
-struct WarpScratch {
-    float from[16], step[16], cfg[16], nn[16], vec[16], next[16];
-    int bad;
-    int pad_[3];
-};
+#include "batch_kernel.cuh"
 
-// Whole warp: check the g points of the edge in W (from + k * step),
-// k = 1..g, in ceil(g / 32) rounds of one point per lane.  Contiguous order
-// gives round r the points 32 r + lane + 1; interleaved order gives it
-// lane * R + r + 1, so the first round already samples the whole edge at
-// stride R and a collision usually ends the edge after one round.  Adds the
-// work done to work[0] (FLOPs) and work[1] (points).
-template <class Gen>
-__device__ __forceinline__ bool warp_validate(const WarpScratch &W, int g, int interleave, CheckCtx &ctx,
-                                              unsigned long long *work)
-{
-    constexpr int D = Gen::kDof;
-    const int lane = lane_id();
-    volatile int *flag = ctx.stop_flag;
-    if (lane == 0) *flag = 0;
-    __syncwarp();
-    bool bad = false;
-    int n = 0;
-    unsigned long long flops = 0;
-    const int R = (g + 31) >> 5;
-    for (int r = 0; r < R; r++) {
-        const int k = interleave ? lane * R + r + 1 : 32 * r + lane + 1;
-        const bool run = k <= g && !*flag;
-        if (run) {
-            float q[D];
-#pragma unroll
-            for (int d = 0; d < D; d++) q[d] = __fadd_rn(W.from[d], __fmul_rn((float)k, W.step[d]));
-            ctx.work = 0;
-            if (!Gen::fkcc(q, ctx)) {
-                bad = true;
-                *flag = 1;
-            }
-            flops += ctx.work + Gen::kFkFlops;
-        }
-        n += __popc(__ballot_sync(0xffffffffu, run));
-        if (__any_sync(0xffffffffu, bad)) break;
-    }
-    flops = warp_sum(flops);
-    if (lane == 0) {
-        atomicAdd(work, flops);
-        atomicAdd(work + 1, (unsigned long long)n);
-    }
-    return !__any_sync(0xffffffffu, bad);
-}
-
-// lane 0 only: finish an unsolved query (first caller wins)
-__device__ __forceinline__ void batch_finish(const BatchParams &P, SlotState *S, int q, int status)
-{
-    if (atomicCAS(&S->state, SLOT_RUNNING, SLOT_DONE) != SLOT_RUNNING) return;
-    BatchOut &o = P.out[q];
-    volatile SlotState *vs = S;
-    o.solved = 0;
-    o.status = status;
-    o.start_tree_size = min(vs->free_index[0], P.cap);
-    o.goal_tree_size = min(vs->free_index[1], P.cap);
-    o.path_length = 0;
-    o.iters = -1;
-    o.cost = 0.0f;
-    o.path_rows = 0;
-    o.samples = vs->ticket;
-    o.t_done = global_ns();
-    __threadfence();
-    atomicAdd(&P.ctr->done, 1);
-}
-
-// lane 0 only: walk a tree from `start` to its root; returns the node count
-// (root excluded) or -1 on a broken chain.
-template <int D>
-__device__ int chain_length(const int *parents, int cap, int start, int *root)
-{
-    const volatile int *vp = parents;
-    int cur = start;
-    for (int n = 0; n <= cap; n++) {
-        const int par = vp[cur];
-        if (par == cur) {
-            *root = cur;
-            return n;
-        }
-        if (par < 0 || par >= cap) return -1;
-        cur = par;
-    }
-    return -1;
-}
-
-// lane 0 only: trace the solution into the path pool in the reference's
-// order (goal, goal-tree segment toward the junction, start-tree segment,
-// start; pRRTC.cu:731-741) and publish the query's result.
-template <int D>
-__device__ void batch_trace(const BatchParams &P, SlotState *S, int s, int q, int t, int jt, int jo, int iter)
-{
-    const float *nodes_s = P.nodes + (size_t)s * 2 * D * P.cap;
-    const int *par_s = P.parents + (size_t)s * 2 * P.cap;
-    const int o = 1 - t;
-    const int j0 = t == 0 ? jt : jo, j1 = t == 0 ? jo : jt;
-    int r0 = 0, r1 = 0;
-    const int n0 = chain_length<D>(par_s, P.cap, j0, &r0);
-    const int n1 = chain_length<D>(par_s + P.cap, P.cap, j1, &r1);
-    BatchOut &out = P.out[q];
-    out.solved = 1;
-    out.iters = iter;
-    out.reached_goal = r1;
-    volatile SlotState *vs = S;
-    out.start_tree_size = min(vs->free_index[0], P.cap);
-    out.goal_tree_size = min(vs->free_index[1], P.cap);
-    out.samples = vs->ticket;
-    if (n0 < 0 || n1 < 0) {
-        out.status = PRRTC_ENOMEM;
-        out.path_rows = 0;
-    } else {
-        const int rows = n0 + n1 + 2;
-        const int off = atomicAdd(&P.ctr->path_next, rows);
-        // cost in the reference's order: the connecting tree first, then the other
-        float cost = 0.0f;
-        for (int pass = 0; pass < 2; pass++) {
-            const int tree = pass == 0 ? t : o;
-            const float *nd = nodes_s + (size_t)tree * D * P.cap;
-            const int *pr = par_s + (size_t)tree * P.cap;
-            int cur = tree == 0 ? j0 : j1;
-            const int n = tree == 0 ? n0 : n1;
-            for (int i = 0; i < n; i++) {
-                const int par = ((const volatile int *)pr)[cur];
-                float acc = 0.0f;
-                const bool write = off + rows <= P.path_pool_rows;
-                const int row = tree == 0 ? off + n1 + 1 + i : off + n1 - i;
-#pragma unroll
-                for (int d = 0; d < D; d++) {
-                    const float a = __ldcg(nd + (size_t)d * P.cap + cur);
-                    const float b = __ldcg(nd + (size_t)d * P.cap + par);
-                    const float df = a - b;
-                    acc = fmaf(df, df, acc);
-                    if (write) P.path_pool[(size_t)row * D + d] = a;
-                }
-                cost += sqrtf(acc);
-                cur = par;
-            }
-        }
-        out.cost = cost;
-        out.path_length = n0 + n1;
-        if (off + rows <= P.path_pool_rows) {
-            const BatchQueryDesc &Q = P.queries[q];
-            const float *start = P.cfg_pool + Q.cfg_off;
-            const float *goal = start + D + (size_t)r1 * D;
-#pragma unroll
-            for (int d = 0; d < D; d++) {
-                P.path_pool[(size_t)off * D + d] = goal[d];
-                P.path_pool[(size_t)(off + rows - 1) * D + d] = start[d];
-            }
-            out.path_off = off;
-            out.path_rows = rows;
-            out.status = 0;
-        } else {
-            out.path_rows = 0;
-            out.status = PRRTC_ENOMEM;
-        }
-    }
-    out.t_done = global_ns();
-    __threadfence();
-    atomicAdd(&P.ctr->done, 1);
-}
-
-// whole warp: write query qa's roots into slot s and start it
-template <int D>
-__device__ void batch_admit(const BatchParams &P, int s, int qa)
-{
-    const int lane = lane_id();
-    const BatchQueryDesc Q = P.queries[qa];
-    float *nodes_s = P.nodes + (size_t)s * 2 * D * P.cap;
-    int *par_s = P.parents + (size_t)s * 2 * P.cap;
-    float *rad_s = P.radii + (size_t)s * 2 * P.cap;
-    const float *cfg = P.cfg_pool + Q.cfg_off;
-    if (lane < D) nodes_s[(size_t)lane * P.cap] = cfg[lane];
-    for (int i = lane; i < Q.num_goals * D; i += 32) {
-        const int g = i / D, d = i % D;
-        nodes_s[(size_t)D * P.cap + (size_t)d * P.cap + g] = cfg[D + i];
-    }
-    for (int g = lane; g < Q.num_goals; g += 32) {
-        par_s[P.cap + g] = g;
-        rad_s[P.cap + g] = FLT_MAX;
-    }
-    if (lane == 0) {
-        par_s[0] = 0;
-        rad_s[0] = FLT_MAX;
-    }
-    if (P.balance == 2)
-        for (int l = lane; l < P.lanes; l += 32) P.tsel[(size_t)s * P.lanes + l] = 0;
-    if (lane == 0) {
-        SlotState *S = &P.slots[s];
-        S->query = qa;
-        S->free_index[0] = 1;
-        S->free_index[1] = Q.num_goals;
-        S->ticket = 0;
-        P.out[qa].t_admit = global_ns();
-    }
-    __threadfence();
-    __syncwarp();
-    if (lane == 0) atomicExch(&P.slots[s].state, SLOT_RUNNING);
-}
-
-// whole warp: restore slot s's used arena prefix to NaN
-template <int D>
-__device__ void batch_scrub(const BatchParams &P, int s)
-{
-    const volatile SlotState *vs = &P.slots[s];
-    float *nodes_s = P.nodes + (size_t)s * 2 * D * P.cap;
-    for (int t = 0; t < 2; t++) {
-        const int n = min(vs->free_index[t], P.cap);
-        float *nd = nodes_s + (size_t)t * D * P.cap;
-        for (int d = 0; d < D; d++)
-            for (int i = lane_id(); i < n; i += 32) nd[(size_t)d * P.cap + i] = __int_as_float(0xFFFFFFFF);
-    }
-    __threadfence();
-    __syncwarp();
-}
-
-// whole warp: leave slot s; the last warp out of a finished slot scrubs it
-// and admits the next pending query (returns true if this warp now works on
-// that newly admitted query).
-template <int D>
-__device__ bool batch_leave(const BatchParams &P, int s, bool allow_admit)
-{
-    const int lane = lane_id();
-    int recycle = 0;
-    if (lane == 0) {
-        __threadfence();
-        SlotState *S = &P.slots[s];
-        const int left = atomicSub(&S->workers, 1) - 1;
-        recycle = left == 0 && atomicCAS(&S->state, SLOT_DONE, SLOT_BUSY) == SLOT_DONE;
-    }
-    recycle = __shfl_sync(0xffffffffu, recycle, 0);
-    if (!recycle) return false;
-    batch_scrub<D>(P, s);
-    int qa = -1;
-    if (lane == 0 && allow_admit) {
-        if (*(volatile int *)&P.ctr->admit_next < P.num_queries) qa = atomicAdd(&P.ctr->admit_next, 1);
-        if (qa >= P.num_queries) qa = -1;
-        if (qa >= 0) atomicAdd(&P.slots[s].workers, 1);
-    }
-    qa = __shfl_sync(0xffffffffu, qa, 0);
-    if (qa >= 0) {
-        batch_admit<D>(P, s, qa);
-        return true;
-    }
-    if (lane == 0) atomicExch(&P.slots[s].state, SLOT_FREE);
-    return false;
-}
-
-template <class Gen>
-__global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
-{
-    constexpr int D = Gen::kDof;
-    constexpr unsigned FULL = 0xffffffffu;
-    extern __shared__ float4 s_raw[];
-    WarpScratch &W = reinterpret_cast<WarpScratch *>(s_raw)[threadIdx.x >> 5];
-    const int lane = lane_id();
-    BatchCounters *C = P.ctr;
-    const float fg = (float)P.granularity;
-    if (lane == 0) atomicCAS(&C->t0, 0ull, global_ns());
-    int slot = -1;
-    unsigned idle = 0;
-
-    while (true) {
-        // ---- time budget
-        int timed_out = 0;
-        if (lane == 0 && P.budget_ns) timed_out = global_ns() - *(volatile unsigned long long *)&C->t0 > P.budget_ns;
-        timed_out = __shfl_sync(FULL, timed_out, 0);
-        if (timed_out) {
-            if (slot >= 0) {
-                if (lane == 0) batch_finish(P, &P.slots[slot], P.slots[slot].query, PRRTC_ETIMEDOUT);
-                __syncwarp();
-                batch_leave<D>(P, slot, false);
-            }
-            return;
-        }
-        // ---- find work
-        if (slot < 0) {
-            int found = -1, admit = -1, rec = -1;
-            if (lane == 0) {
-                const unsigned s0 = atomicAdd((unsigned *)&C->cursor, 1u);
-                for (int tries = 0; tries < P.num_slots && found < 0 && rec < 0; tries++) {
-                    const int s = (int)((s0 + (unsigned)tries) % (unsigned)P.num_slots);
-                    SlotState *S = &P.slots[s];
-                    const int st = *(volatile int *)&S->state;
-                    if (st == SLOT_RUNNING) {
-                        atomicAdd(&S->workers, 1);
-                        if (*(volatile int *)&S->state == SLOT_RUNNING) {
-                            found = s;
-                        } else {
-                            rec = s;      // leave it again (possibly recycling it)
-                        }
-                    } else if (st == SLOT_FREE && *(volatile int *)&C->admit_next < P.num_queries) {
-                        if (atomicCAS(&S->state, SLOT_FREE, SLOT_BUSY) == SLOT_FREE) {
-                            const int qa = atomicAdd(&C->admit_next, 1);
-                            if (qa < P.num_queries) {
-                                atomicAdd(&S->workers, 1);
-                                found = s;
-                                admit = qa;
-                            } else {
-                                atomicExch(&S->state, SLOT_FREE);
-                            }
-                        }
-                    }
-                }
-            }
-            found = __shfl_sync(FULL, found, 0);
-            admit = __shfl_sync(FULL, admit, 0);
-            rec = __shfl_sync(FULL, rec, 0);
-            if (rec >= 0) {
-                if (batch_leave<D>(P, rec, true)) {
-                    slot = rec;
-                    idle = 0;
-                }
-                continue;
-            }
-            if (found < 0) {
-                int all_done = 0;
-                if (lane == 0) all_done = *(volatile int *)&C->done >= P.num_queries;
-                if (__shfl_sync(FULL, all_done, 0)) return;
-                if (++idle > (1u << 22)) {
-                    if (lane == 0) atomicOr(&C->error, 1);
-                    return;
-                }
-                __nanosleep(256);
-                continue;
-            }
-            if (admit >= 0) batch_admit<D>(P, found, admit);
-            slot = found;
-            idle = 0;
-        }
-
-        // ---- one RRT-Connect iteration on `slot`
-        SlotState *S = &P.slots[slot];
-        const int q = *(volatile int *)&S->query;
-        const BatchQueryDesc Qd = P.queries[q];
-        CheckCtx ctx{{Qd.env, Qd.env_n}, P.pad, &W.bad};
-        float *nodes_s = P.nodes + (size_t)slot * 2 * D * P.cap;
-        int *par_s = P.parents + (size_t)slot * 2 * P.cap;
-        float *rad_s = P.radii + (size_t)slot * 2 * P.cap;
-
-        int k = 0;
-        if (lane == 0) k = atomicAdd(&S->ticket, 1);
-        k = __shfl_sync(FULL, k, 0);
-        const int vl = k % P.lanes;
-        const int iter = k / P.lanes + 1;
-        if ((long long)k >= P.max_samples_drawn) {
-            if (lane == 0) batch_finish(P, S, q, 0);
-        } else {
-            int t = 0;
-            if (lane == 0) {
-                volatile SlotState *vs = S;
-                const int f0 = vs->free_index[0], f1 = vs->free_index[1];
-                const int L = P.lanes;
-                if (P.balance == 0 || iter == 1) {
-                    t = (vl < (L / 2)) ? 0 : 1;
-                } else if (P.balance == 1 && 2 * abs(f0 - f1) < 3 * L) {
-                    const float ratio = f0 / (float)(f0 + f1);
-                    t = ((float)vl < L * (1.0f - ratio)) ? 0 : 1;
-                } else if (P.balance == 1) {
-                    const float ratio = f0 / (float)(f0 + f1);
-                    t = ratio < P.tree_ratio ? 0 : 1;
-                } else {
-                    int *ts = P.tsel + (size_t)slot * L + vl;
-                    t = *(volatile int *)ts;
-                    const int ft = t == 0 ? f0 : f1, fo = t == 0 ? f1 : f0;
-                    const float ratio = abs(ft - fo) / (float)ft;
-                    if (ratio < P.tree_ratio) t = 1 - t;
-                    *ts = t;
-                }
-                if (P.balance == 2 && iter == 1) P.tsel[(size_t)slot * L + vl] = t;
-            }
-            t = __shfl_sync(FULL, t, 0);
-            const int o = 1 - t;
-            float *nd_t = nodes_s + (size_t)t * D * P.cap, *nd_o = nodes_s + (size_t)o * D * P.cap;
-            int *pr_t = par_s + (size_t)t * P.cap;
-            float *rd_t = rad_s + (size_t)t * P.cap;
-            if (lane < D) {
-                const float h = radical_inverse((unsigned)iter, (unsigned)P.halton_bases[vl * 16 + lane]);
-                W.cfg[lane] = fmaf(h, P.scale[lane], P.offset[lane]);
-            }
-            __syncwarp();
-            float qv[D];
-#pragma unroll
-            for (int d = 0; d < D; d++) qv[d] = W.cfg[d];
-            float dsq;
-            int ni;
-            const int cnt_t = *(volatile int *)&S->free_index[t];
-            warp_nn<D>(nd_t, P.cap, cnt_t, qv, dsq, ni);
-            if (lane == 0) atomicAdd(&C->nn_nodes, (unsigned long long)min(cnt_t, P.cap));
-            const float dist = sqrtf(dsq);
-            const float scale = fminf(1.0f, P.range / dist);
-            int skip = 0;
-            if (lane == 0) skip = P.dynamic_domain && __ldcg(rd_t + ni) < dist;
-            skip = __shfl_sync(FULL, skip, 0);
-            if (!skip) {
-                if (lane < D) {
-                    const float nn = __ldcg(nd_t + (size_t)lane * P.cap + ni);
-                    const float c = fmaf(W.cfg[lane] - nn, scale, nn);
-                    W.nn[lane] = nn;
-                    W.from[lane] = nn;
-                    W.cfg[lane] = c;
-                    W.step[lane] = __fdiv_rn(__fsub_rn(c, nn), fg);
-                }
-                __syncwarp();
-                if (!warp_validate<Gen>(W, P.granularity, P.edge_order, ctx, C->work)) {
-                    if (lane == 0 && P.dynamic_domain) dd_shrink(rd_t + ni, P.dd_alpha, P.dd_radius, P.dd_min_radius);
-                } else {
-                    int idx = -1;
-                    if (lane == 0) {
-                        idx = atomicAdd(&S->free_index[t], 1);
-                        if (idx >= P.max_samples || idx >= P.cap) {
-                            batch_finish(P, S, q, idx >= P.max_samples ? 0 : PRRTC_ENOMEM);
-                            idx = -1;
-                        } else {
-                            pr_t[idx] = ni;
-                            if (P.dynamic_domain) {
-                                rd_t[idx] = FLT_MAX;
-                                dd_grow(rd_t + ni, P.dd_alpha);
-                            }
-                        }
-                    }
-                    idx = __shfl_sync(FULL, idx, 0);
-                    if (idx >= 0) {
-                        if (lane < D) nd_t[(size_t)lane * P.cap + idx] = W.cfg[lane];
-                        __threadfence();
-                        __syncwarp();
-                        // connect toward the other tree
-#pragma unroll
-                        for (int d = 0; d < D; d++) qv[d] = W.cfg[d];
-                        int oi;
-                        const int cnt_o = *(volatile int *)&S->free_index[o];
-                        warp_nn<D>(nd_o, P.cap, cnt_o, qv, dsq, oi);
-                        if (lane == 0) atomicAdd(&C->nn_nodes, (unsigned long long)min(cnt_o, P.cap));
-                        const unsigned n_ext = (unsigned)ceilf(sqrtf(dsq) / P.range);
-                        if (lane < D) W.vec[lane] = (__ldcg(nd_o + (size_t)lane * P.cap + oi) - W.cfg[lane]) / (float)n_ext;
-                        __syncwarp();
-                        unsigned i_ext = 0;
-                        int parent = idx;
-                        while (i_ext < n_ext) {
-                            if (lane < D) {
-                                const float a = W.cfg[lane];
-                                const float b = a + W.vec[lane];
-                                W.next[lane] = b;
-                                W.from[lane] = a;
-                                W.step[lane] = __fdiv_rn(__fsub_rn(b, a), fg);
-                            }
-                            __syncwarp();
-                            if (!warp_validate<Gen>(W, P.granularity, P.edge_order, ctx, C->work)) break;
-                            int idx2 = -1;
-                            if (lane == 0) {
-                                idx2 = atomicAdd(&S->free_index[t], 1);
-                                if (idx2 >= P.max_samples || idx2 >= P.cap) {
-                                    batch_finish(P, S, q, idx2 >= P.max_samples ? 0 : PRRTC_ENOMEM);
-                                    idx2 = -1;
-                                } else {
-                                    pr_t[idx2] = parent;
-                                    rd_t[idx2] = FLT_MAX;
-                                }
-                            }
-                            idx2 = __shfl_sync(FULL, idx2, 0);
-                            if (idx2 < 0) {
-                                parent = -1;
-                                break;
-                            }
-                            if (lane < D) {
-                                W.cfg[lane] = W.next[lane];
-                                nd_t[(size_t)lane * P.cap + idx2] = W.next[lane];
-                            }
-                            __threadfence();
-                            __syncwarp();
-                            parent = idx2;
-                            i_ext++;
-                        }
-                        if (i_ext == n_ext && parent >= 0 && lane == 0) {
-                            if (atomicCAS(&S->state, SLOT_RUNNING, SLOT_DONE) == SLOT_RUNNING) {
-                                __threadfence();
-                                batch_trace<D>(P, S, slot, q, t, parent, oi, iter);
-                            }
-                        }
-                        __syncwarp();
-                    }
-                }
-            }
-        }
-        // ---- leave a finished slot
-        int st = 0;
-        if (lane == 0) st = *(volatile int *)&S->state;
-        st = __shfl_sync(FULL, st, 0);
-        if (st != SLOT_RUNNING) {
-            if (!batch_leave<D>(P, slot, true)) slot = -1;
-        }
-    }
-}
+namespace prrtc {
 
 inline int grid_for(int64_t work, int threads, int sms, int per_sm)
 {

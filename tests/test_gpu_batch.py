@@ -52,7 +52,8 @@ def test_batch_shelf_dd_balance2(ctx, oracle):
 def test_batch_admission_graph_and_reruns(ctx, oracle):
     from prrtc_gb300 import BatchSettings
     qs = queries("fetch", "mixed", 40, 100, 20)
-    b = ctx.batch("fetch", qs, BatchSettings(c0(granularity=64, balance=1, tree_ratio=0.5), max_active=7, use_graph=1))
+    b = ctx.batch("fetch", qs, BatchSettings(c0(granularity=64, balance=1, tree_ratio=0.5), max_active=7, use_graph=1,
+                                              max_attempts=1))
     for _ in range(3):
         b.run()
         res = b.results()
@@ -93,3 +94,16 @@ def test_batch_time_budget_and_iteration_limit(ctx):
     # the arena is clean again: a normal batch still solves everything
     res = ctx.solve_batch("panda", qs[:8], BatchSettings(c0()))
     assert all(r.solved for r in res)
+
+
+def test_batch_attempts_and_restarts(ctx, oracle):
+    """Extra attempts (idle warps in the tail) and restarts (an attempt that
+    exhausts its arena) keep every returned path valid and solve as many."""
+    from prrtc_gb300 import BatchSettings
+    qs = queries("panda", "shelf", 24, 300)
+    base = c0(granularity=64, balance=2, tree_ratio=1.0, dynamic_domain=True, range=0.5)
+    for kw in (dict(max_attempts=1), dict(max_attempts=8, restart_after_ns=100000, max_workers_per_attempt=4),
+               dict(max_attempts=8, max_nodes_per_tree=256, restart_after_ns=100000)):
+        res = ctx.solve_batch("panda", qs, BatchSettings(base, **kw))
+        solved = check_all(oracle, "panda", qs, res, 64, need_all=False)
+        assert solved >= (24 if kw.get("max_nodes_per_tree") is None else 12), kw
