@@ -53,6 +53,7 @@ WORKLOAD_SETTINGS = {
 MARGIN = 1e-5   # planning margin (m): every returned path clears contact by 10 micrometres
 GPU_BUDGET_NS = int(30e9)   # per batch launch; unsolved queries past it count as failures
 CPU_BUDGET_S = 20.0         # per query in the CPU restatement
+PLAIN_BUDGET_S = 30.0       # total for the plain-form comparison
 
 
 def log(*a):
@@ -155,15 +156,18 @@ def reference_arm(args, rank, world):
 
 
 def metric_name(args):
-    return f"solved queries/s, batched, {args.queries} {args.workload} queries (1 GB300, 100% revalidated)"
+    return f"solved queries/s, batched, {args.workload} ({args.queries} queries per step; 1 GB300, 100% revalidated)"
 
 
 def config_of(args):
     from prrtc_gb300 import autotune, workloads
-    return {"workload": f"{args.workload}_{args.queries}", "queries": args.queries,
+    return {"workload": f"{args.workload}_{args.queries}", "queries_per_step": args.queries,
+            "steps_streamed": "the K steps' queries (distinct seeds) flow through one persistent launch with "
+                              f"{args.queries} resident slots; queries are admitted as others finish",
             "settings": WORKLOAD_SETTINGS[args.workload], "planning_margin_m": MARGIN,
             "batch_shape": autotune.load(workloads.WORKLOADS[args.workload][0], args.workload),
-            "l2": "flushed between steps (256 MiB write)", "parallelism": "queries sharded over ranks"}
+            "l2": "flushed before the timed launch; each step's queries use fresh arena slots and scenes "
+                  "(stream input > L2)", "parallelism": "queries sharded over ranks"}
 
 
 def h2d_bytes(qs):
@@ -183,37 +187,42 @@ def ours(args, rank, world):
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
     robot = workloads.WORKLOADS[args.workload][0]
-    qs = workloads.make(args.workload, args.queries, seed0=rank * args.queries)
+    n = args.queries
+    # K steps of n queries each, distinct seeds, streamed through one launch
+    qs = workloads.make(args.workload, n * args.steps, seed0=rank * n * args.steps)
+    first = qs[:n]
     plan = settings_for(args.workload)
     ctx = Context(dev)
     envs = [ctx.upload_env(q.env) for q in qs]
     tuned = autotune.load(robot, args.workload)
-    bs = BatchSettings(plan, use_graph=1, margin=MARGIN, time_budget_ns=GPU_BUDGET_NS, **tuned)
-    batch = ctx.batch(robot, [(e, q.start, q.goal) for e, q in zip(envs, qs)], bs, path_capacity=2048)
+    common = dict(use_graph=1, margin=MARGIN, time_budget_ns=GPU_BUDGET_NS, **tuned)
+    stream = ctx.batch(robot, [(e, q.start, q.goal) for e, q in zip(envs, qs)],
+                       BatchSettings(plan, max_active=n, **common), path_capacity=2048)
+    single = ctx.batch(robot, [(e, q.start, q.goal) for e, q in zip(envs[:n], first)], BatchSettings(plan, **common),
+                       path_capacity=2048)
     flush = torch.empty(64 << 20, dtype=torch.float32, device=f"cuda:{dev}")
-    launches0 = ctx.launches
+    # warm-up: the first step's batch on its own, W times (also the one-batch figures)
+    single_ms, single_solved = [], []
     for _ in range(args.warmup):
-        batch.run()
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        single.run()
+        res1 = single.results()
+        single_ms.append(single.stats()["kernel_ns"] / 1e6)
+        single_solved.append(sum(r.solved for r in res1))
     if world > 1:
         torch.distributed.barrier()
+    flush.fill_(1.0)
     torch.cuda.synchronize()
-    kernel_ns, solved, flops, cfgs, nn_nodes, results = 0, 0, 0, 0, 0, None
     launches0 = ctx.launches
     with ClockSampler(dev) as clk:
-        for _ in range(args.steps):
-            flush.fill_(1.0)
-            torch.cuda.synchronize()
-            batch.run()
-            st = batch.stats()
-            kernel_ns += st["kernel_ns"]
-            flops += st["flops"]
-            cfgs += st["configs_checked"]
-            nn_nodes += st["nn_nodes"]
-            results = batch.results()
-            solved += sum(r.solved for r in results)
-    torch.cuda.synchronize()
+        stream.run()
+        torch.cuda.synchronize()
     launches = ctx.launches - launches0
-    t_dev = kernel_ns * 1e-9
+    st = stream.stats()
+    results = stream.results()
+    solved = sum(r.solved for r in results)
+    t_dev = st["kernel_ns"] * 1e-9
     if world > 1:
         t = torch.tensor([t_dev], device=f"cuda:{dev}")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -224,67 +233,73 @@ def ours(args, rank, world):
     value = solved / t_dev
     lat = [r.kernel_ns / 1e6 for r in results if r.solved]
 
-    # ---- e2e through the C ABI with host buffers
-    e2e_solved, e2e_t = 0, 0.0
+    # ---- e2e through the C ABI with host buffers (same streamed job)
     host_q = [(q.env, q.start, q.goal) for q in qs]
-    ctx.solve_batch(robot, host_q[:64], bs)
-    for _ in range(args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        res = ctx.solve_batch(robot, host_q, bs, path_capacity=2048)
-        e2e_t += time.perf_counter() - t0
-        e2e_solved += sum(r.solved for r in res)
-    d2h = sum(len(r.path) * r.path.shape[1] * 4 for r in res) + 64 * len(res)
+    bs_host = BatchSettings(plan, max_active=n, **common)
+    ctx.solve_batch(robot, host_q[:64], BatchSettings(plan, **common))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res_e2e = ctx.solve_batch(robot, host_q, bs_host, path_capacity=2048)
+    e2e_t = time.perf_counter() - t0
+    e2e_solved = sum(r.solved for r in res_e2e)
+    d2h = sum(len(r.path) * r.path.shape[1] * 4 for r in res_e2e) + 64 * len(res_e2e)
 
     if rank != 0:
         return
-    # ---- revalidation of every returned path (last timed step) by the oracle checker
+    # ---- revalidation of every returned path by the oracle checker
     O = oracle_lib()
     g = plan.granularity
-    bad = 0
-    for q, r in zip(qs, results):
-        if r.solved and not O.check_edges(robot, q.env, r.path[:-1], r.path[1:], g).all():
-            bad += 1
-    n_solved_last = sum(r.solved for r in results)
+    bad = sum(1 for q, r in zip(qs, results)
+              if r.solved and not O.check_edges(robot, q.env, r.path[:-1], r.path[1:], g).all())
 
-    # ---- the plain single-query form on a sample
-    ns_plain = min(64, len(qs))
+    # ---- the plain single-query form on the first step's queries, one at a time
     plain_t, plain_solved, plain_ms = 0.0, 0, []
     ctx.set_planning_margin(MARGIN)
-    for q, e in zip(qs[:ns_plain], envs[:ns_plain]):
+    ctx.set_time_budget(int(GPU_BUDGET_NS))
+    for q, e in zip(first, envs[:n]):
         r = ctx.solve(robot, q.start, q.goal, e, plan)
         plain_t += r.wall_ns * 1e-9
         plain_solved += r.solved
         plain_ms.append(r.wall_ns / 1e6)
+        if plain_t > PLAIN_BUDGET_S:
+            break
+    ns_plain = len(plain_ms)
     plain_qps = plain_solved / plain_t
 
     # ---- roofline: FP32 work of the planner kernel vs the measured FP32 peak
     peak = ctx.measure_fp32_peak()
-    achieved = flops / t_dev / 1e12
-    nn_bytes = nn_nodes * 4 * plan_dof(robot)
+    achieved = st["flops"] / (st["kernel_ns"] * 1e-9) / 1e12
+    nn_bytes = st["nn_nodes"] * 4 * plan_dof(robot)
 
     # ---- CPU baseline (bounded sample)
     ns_cpu = min(cpu_sample_size(args.workload), len(qs))
     threads = os.cpu_count() or 1
     cs, cdt, _ = cpu_planner(robot, qs[:ns_cpu], plan, threads)
 
+    single_med = statistics.median(single_ms)
     line = {
         "metric": metric_name(args), "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_of(args),
         "p50_solve_ms": statistics.median(lat) if lat else None,
         "p99_solve_ms": float(np.percentile(lat, 99)) if lat else None,
-        "success_rate": n_solved_last / len(qs), "revalidated": f"{n_solved_last - bad}/{n_solved_last}",
-        "edge_validations_per_s": cfgs / plan.granularity / t_dev,
-        "configs_per_s": cfgs / t_dev,
-        "plain": {"queries_per_s": plain_qps, "p50_solve_ms": statistics.median(plain_ms), "sample": ns_plain,
-                  "batched_over_plain": value / plain_qps},
-        "e2e": {"value": e2e_solved / e2e_t, "unit": "queries/s", "h2d_bytes_per_step": h2d_bytes(qs),
-                "d2h_bytes_per_step": d2h},
+        "max_solve_ms": max(lat) if lat else None,
+        "success_rate": solved / len(qs), "revalidated": f"{solved - bad}/{solved}",
+        "edge_validations_per_s": st["configs_checked"] / g / (st["kernel_ns"] * 1e-9),
+        "configs_per_s": st["configs_checked"] / (st["kernel_ns"] * 1e-9),
+        "extra_attempts": st["extra_attempts"],
+        "one_batch": {"queries": n, "ms_median": single_med, "ms_all": single_ms,
+                      "queries_per_s": statistics.median(single_solved) / (single_med * 1e-3),
+                      "note": "the first step's queries alone in one launch: its time is its slowest query's"},
+        "plain": {"queries_per_s": plain_qps, "p50_solve_ms": statistics.median(plain_ms),
+                  "max_solve_ms": max(plain_ms), "sample": f"{ns_plain} of the first step's {n} queries",
+                  "solved": plain_solved, "batched_over_plain": value / plain_qps},
+        "e2e": {"value": e2e_solved / e2e_t, "unit": "queries/s", "h2d_bytes_per_step": h2d_bytes(qs) // args.steps,
+                "d2h_bytes_per_step": d2h // args.steps},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
                      "peak_source": "measured FP32 FMA chain kernel on this GPU (prrtc_measure_fp32_peak)",
-                     "nn_scan_bytes_per_s": nn_bytes / t_dev},
+                     "nn_scan_bytes_per_s": nn_bytes / (st["kernel_ns"] * 1e-9)},
         "cpu_baseline": {"value": cs / cdt, "unit": "queries/s", "cores": threads, "kind": "port",
                          "sample": f"first {ns_cpu} of the {len(qs)} queries, oracle RRT-Connect restatement"},
         "gpu_launches": launches,

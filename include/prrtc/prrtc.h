@@ -209,14 +209,14 @@ typedef struct prrtc_batch_settings {
                                         modes see the lane as pRRTC sees blockIdx.x.  0: 2.  pRRTC's
                                         own count (plan.num_new_configs) reproduces its sample set,
                                         whose first points cluster near the lower joint limits */
-    int max_nodes_per_tree;          /* arena capacity per tree (0: min(max_samples, 32768)) */
+    int max_nodes_per_tree;          /* arena capacity per tree (0: min(max_samples, 65536)) */
     int max_active;                  /* resident query slots (0: all queries, within the arena budget) */
     int warps_per_block;             /* 0: 4 */
     int edge_order;                  /* order a warp checks an edge's points in: 0 contiguous
                                         rounds, 1 interleaved (every round spans the edge) */
     int sampler;                     /* 0: pRRTC's Halton lanes; 1: Halton with per-query digit
                                         scrambling and rotation (decorrelates large bases) */
-    int max_attempts;                /* independent attempts per query (0: 64; 1: none).  An attempt
+    int max_attempts;                /* independent attempts per query (0: 4; 1: none).  An attempt
                                         that runs out of samples or arena restarts the query; once
                                         no query is pending, idle warps open extra attempts of
                                         queries running longer than k x restart_after_ns; the first

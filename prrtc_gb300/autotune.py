@@ -12,6 +12,9 @@ Sweeps, on a calibration batch of seeded queries, the knobs of
                        Halton;
 * ``max_workers_per_attempt``  warps per attempt before idle warps open
                        independent attempts (the tail's portfolio);
+* ``max_attempts``     attempts per query, fixed at 4: restarting an attempt
+                       that exhausted its arena costs nothing until it happens,
+                       so it is a robustness setting rather than a speed knob;
 
 and keeps the setting with the highest solved queries per second.  Results
 are cached in ``tuning.json`` next to this file, keyed by robot and workload:
@@ -26,9 +29,10 @@ import sys
 from pathlib import Path
 
 TUNING = Path(__file__).resolve().parent / "tuning.json"
-DEFAULT = {"lanes": 2, "warps_per_block": 2, "edge_order": 0, "sampler": 1, "max_workers_per_attempt": 32}
-SPACE = {"lanes": (1, 2, 4), "warps_per_block": (2,), "edge_order": (0,), "sampler": (0, 1),
-         "max_workers_per_attempt": (16, 32, 64)}
+DEFAULT = {"lanes": 1, "warps_per_block": 2, "edge_order": 0, "sampler": 0, "max_workers_per_attempt": 0,
+           "max_attempts": 4}
+SPACE = {"lanes": (1, 2), "warps_per_block": (2,), "edge_order": (0,), "sampler": (0, 1),
+         "max_workers_per_attempt": (64, 256, 0), "max_attempts": (4,)}
 KNOBS = tuple(SPACE)
 
 
@@ -79,7 +83,7 @@ def main(argv):
     name = argv[1] if len(argv) > 1 else "panda_shelf"
     n = int(argv[2]) if len(argv) > 2 else 1024
     robot = workloads.WORKLOADS[name][0]
-    qs = workloads.make(name, n, seed0=10_000)     # calibration queries, disjoint from the benchmark's
+    qs = workloads.make(name, n, seed0=100_000)    # calibration queries, disjoint from the benchmark's
     ctx = Context(0)
     envs = [ctx.upload_env(q.env) for q in qs]
     out = tune(ctx, robot, [(e, q.start, q.goal) for e, q in zip(envs, qs)], Settings(**WORKLOAD_SETTINGS[name]))

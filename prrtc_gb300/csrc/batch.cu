@@ -139,7 +139,7 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     cudaSetDevice(c->device);
     *out = nullptr;
     const int D = ops->dof;
-    int cap = settings->max_nodes_per_tree > 0 ? settings->max_nodes_per_tree : std::min(S.max_samples, 32768);
+    int cap = settings->max_nodes_per_tree > 0 ? settings->max_nodes_per_tree : std::min(S.max_samples, 65536);
     cap = std::max(4, (std::min(cap, S.max_samples) + 3) & ~3);
     // pack queries
     std::vector<float> cfg;
@@ -179,8 +179,8 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     b->use_graph = settings->use_graph != 0;
     b->wpb = settings->warps_per_block > 0 ? settings->warps_per_block : 4;
     const size_t slot_bytes = (size_t)2 * cap * (D + 2) * sizeof(float);
-    const size_t arena_budget = (size_t)16 << 30;
-    const int max_attempts = settings->max_attempts > 0 ? settings->max_attempts : 64;
+    const size_t arena_budget = (size_t)32 << 30;
+    const int max_attempts = settings->max_attempts > 0 ? settings->max_attempts : 4;
     int slots = settings->max_active > 0 ? std::min(settings->max_active, n) : n;
     if (max_attempts > 1) slots += std::max(64, n / 4);   // room for extra attempts in the tail
     slots = (int)std::max<size_t>(1, std::min<size_t>(slots, arena_budget / slot_bytes));

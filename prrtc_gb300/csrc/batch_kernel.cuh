@@ -28,6 +28,7 @@ namespace prrtc {
 
 struct WarpScratch {
     float from[16], step[16], cfg[16], nn[16], vec[16], next[16];
+    float chunk[16][33];   // 32 tree nodes staged for the round's nearest-neighbour pass (+1: bank skew)
     int bad;
     int pad_[3];
 };
@@ -358,6 +359,11 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
     if (lane == 0) atomicCAS(&C->t0, 0ull, global_ns());
     int slot = -1;
     unsigned idle = 0;
+    unsigned long long nn_visits = 0;   // flushed once per warp (a shared counter would serialise)
+    auto flush = [&]() {
+        if (lane == 0 && nn_visits) atomicAdd(&C->nn_nodes, nn_visits);
+        nn_visits = 0;
+    };
 
     while (true) {
         // ---- time budget
@@ -370,6 +376,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                 __syncwarp();
                 batch_leave<D>(P, slot, false);
             }
+            flush();
             return;
         }
         // ---- find work: a pending query, else a running attempt with room for
@@ -454,9 +461,13 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
             if (found < 0) {
                 int all_done = 0;
                 if (lane == 0) all_done = vload(&C->done) >= P.num_queries;
-                if (__shfl_sync(FULL, all_done, 0)) return;
+                if (__shfl_sync(FULL, all_done, 0)) {
+                    flush();
+                    return;
+                }
                 if (++idle > (1u << 22)) {
                     if (lane == 0) atomicOr(&C->error, 1);
+                    flush();
                     return;
                 }
                 __nanosleep(256);
@@ -467,7 +478,11 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
             idle = 0;
         }
 
-        // ---- one RRT-Connect iteration on `slot`
+        // ---- one round of up to 32 samples on `slot`: every lane draws a
+        // sample, one shared pass over each tree finds all their nearest
+        // nodes, and the samples that pass the dynamic-domain test are then
+        // extended one at a time by the whole warp (32 of pRRTC's lanes
+        // reading one tree snapshot, pRRTC.cu:378-427)
         SlotState *S = &P.slots[slot];
         const int q = vload(&S->query);
         const int attempt = vload(&S->attempt);
@@ -477,85 +492,123 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
         int *par_s = P.parents + (size_t)slot * 2 * P.cap;
         float *rad_s = P.radii + (size_t)slot * 2 * P.cap;
 
-        int k = 0, qdone = 0;
+        int k0 = 0, qdone = 0, f0 = 0, f1 = 0;
         if (lane == 0) {
             qdone = vload(&P.qstate[q].state) == 2;
             if (qdone) {
                 // another attempt finished the query: cancel this one
                 if (atomicCAS(&S->state, SLOT_RUNNING, SLOT_DONE) == SLOT_RUNNING) atomicSub(&P.qstate[q].live, 1);
             } else {
-                k = atomicAdd(&S->ticket, 1);
+                k0 = atomicAdd(&S->ticket, 32);
+                f0 = vload(&S->free_index[0]);
+                f1 = vload(&S->free_index[1]);
             }
         }
         qdone = __shfl_sync(FULL, qdone, 0);
-        k = __shfl_sync(FULL, k, 0);
-        const int vl = k % P.lanes;
-        const int iter = k / P.lanes + 1;
-        if (qdone) {
-            // leave below
-        } else if ((long long)k >= P.max_samples_drawn) {
+        k0 = __shfl_sync(FULL, k0, 0);
+        f0 = __shfl_sync(FULL, f0, 0);
+        f1 = __shfl_sync(FULL, f1, 0);
+        if (!qdone && (long long)k0 >= P.max_samples_drawn) {
             if (lane == 0) finish_attempt(P, S, q, 0);
-        } else {
-            int t = 0;
-            if (lane == 0) {
-                volatile SlotState *vs = S;
-                const int f0 = vs->free_index[0], f1 = vs->free_index[1];
-                const int L = P.lanes;
-                if (P.balance == 0 || iter == 1) {
-                    t = (vl < (L / 2)) ? 0 : 1;
-                } else if (P.balance == 1 && 2 * abs(f0 - f1) < 3 * L) {
-                    const float ratio = f0 / (float)(f0 + f1);
-                    t = ((float)vl < L * (1.0f - ratio)) ? 0 : 1;
-                } else if (P.balance == 1) {
-                    const float ratio = f0 / (float)(f0 + f1);
-                    t = ratio < P.tree_ratio ? 0 : 1;
-                } else {
-                    // vamp balance (pRRTC.cu:364-371): a lane swaps trees unless the
-                    // other is much larger.  The lane's previous tree is taken as
-                    // alternating from its first choice, so no per-lane state is
-                    // shared by the warps working on the attempt.
-                    const int prev = ((iter - 1) + (vl < (L / 2) ? 0 : 1)) & 1;
-                    const int ft = prev == 0 ? f0 : f1, fo = prev == 0 ? f1 : f0;
-                    const float ratio = abs(ft - fo) / (float)ft;
-                    t = ratio < P.tree_ratio ? 1 - prev : prev;
-                }
+        } else if (!qdone) {
+            // -- this lane's sample
+            const int k = k0 + lane;
+            const bool valid = (long long)k < P.max_samples_drawn;
+            const int vl = k % P.lanes;
+            const int iter = k / P.lanes + 1;
+            const int L = P.lanes;
+            int t;
+            if (P.balance == 0 || iter == 1) {
+                t = (vl < (L / 2)) ? 0 : 1;
+            } else if (P.balance == 1 && 2 * abs(f0 - f1) < 3 * L) {
+                const float ratio = f0 / (float)(f0 + f1);
+                t = ((float)vl < L * (1.0f - ratio)) ? 0 : 1;
+            } else if (P.balance == 1) {
+                const float ratio = f0 / (float)(f0 + f1);
+                t = ratio < P.tree_ratio ? 0 : 1;
+            } else {
+                // vamp balance (pRRTC.cu:364-371): a lane swaps trees unless the
+                // other is much larger.  The lane's previous tree is taken as
+                // alternating from its first choice, so no per-lane state is
+                // shared by the warps working on the attempt.
+                const int prev = ((iter - 1) + (vl < (L / 2) ? 0 : 1)) & 1;
+                const int ft = prev == 0 ? f0 : f1, fo = prev == 0 ? f1 : f0;
+                const float ratio = abs(ft - fo) / (float)ft;
+                t = ratio < P.tree_ratio ? 1 - prev : prev;
             }
-            t = __shfl_sync(FULL, t, 0);
-            const int o = 1 - t;
-            float *nd_t = nodes_s + (size_t)t * D * P.cap, *nd_o = nodes_s + (size_t)o * D * P.cap;
-            int *pr_t = par_s + (size_t)t * P.cap;
-            float *rd_t = rad_s + (size_t)t * P.cap;
-            if (lane < D) {
+            float qv[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) {
                 float h;
                 if (P.sampler == 0) {
                     const int row = (vl + attempt * P.lanes) % P.bases_lanes;
-                    h = radical_inverse((unsigned)iter, (unsigned)P.halton_bases[row * 16 + lane]);
+                    h = radical_inverse((unsigned)iter, (unsigned)P.halton_bases[row * 16 + d]);
                 } else {
                     // scrambled Halton: digit multiplier and rotation per (query, attempt, dimension)
-                    const unsigned b = (unsigned)P.halton_bases[vl % P.bases_lanes * 16 + lane];
+                    const unsigned b = (unsigned)P.halton_bases[vl % P.bases_lanes * 16 + d];
                     const unsigned hs = hash32((unsigned)q * 0x9E3779B1u + (unsigned)attempt * 0xC2B2AE35u +
-                                               (unsigned)lane * 0x85EBCA77u + 0x165667B1u);
+                                               (unsigned)d * 0x85EBCA77u + 0x165667B1u);
                     h = scrambled_radical_inverse((unsigned)iter, b, 1u + hs % (b - 1u));
                     h += (float)(hs >> 8) * (1.0f / 16777216.0f);
                     h -= floorf(h);
                 }
-                W.cfg[lane] = fmaf(h, P.scale[lane], P.offset[lane]);
+                qv[d] = fmaf(h, P.scale[d], P.offset[d]);
             }
-            __syncwarp();
-            float qv[D];
+            // -- nearest node of every lane's sample: one pass per tree, nodes
+            // staged 32 at a time in shared memory and read by all lanes
+            float best = FLT_MAX;
+            int bi = 0;
+            for (int tree = 0; tree < 2; tree++) {
+                if (!__any_sync(FULL, valid && t == tree)) continue;
+                const int cnt = min(tree == 0 ? f0 : f1, P.cap);
+                const float *nd = nodes_s + (size_t)tree * D * P.cap;
+                for (int base = 0; base < cnt; base += 32) {
+                    const int i = base + lane;
 #pragma unroll
-            for (int d = 0; d < D; d++) qv[d] = W.cfg[d];
-            float dsq;
-            int ni;
-            const int cnt_t = vload(&S->free_index[t]);
-            warp_nn<D>(nd_t, P.cap, cnt_t, qv, dsq, ni);
-            if (lane == 0) atomicAdd(&C->nn_nodes, (unsigned long long)min(cnt_t, P.cap));
-            const float dist = sqrtf(dsq);
-            const float scale = fminf(1.0f, P.range / dist);
-            int skip = 0;
-            if (lane == 0) skip = P.dynamic_domain && __ldcg(rd_t + ni) < dist;
-            skip = __shfl_sync(FULL, skip, 0);
-            if (!skip) {
+                    for (int d = 0; d < D; d++) W.chunk[d][lane] = i < cnt ? __ldcg(nd + (size_t)d * P.cap + i) : __int_as_float(0x7FFFFFFF);
+                    __syncwarp();
+                    if (valid && t == tree) {
+                        const int m = min(32, cnt - base);
+                        for (int n = 0; n < m; n++) {
+                            float a = 0.0f;
+#pragma unroll
+                            for (int d = 0; d < D; d++) {
+                                const float x = W.chunk[d][n] - qv[d];
+                                a = fmaf(x, x, a);
+                            }
+                            if (a < best) {
+                                best = a;
+                                bi = base + n;
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
+                nn_visits += (unsigned long long)cnt * __popc(__ballot_sync(FULL, valid && t == tree));
+            }
+            const float dist = sqrtf(best);
+            bool go = valid;
+            if (go && P.dynamic_domain) go = !(__ldcg(rad_s + (size_t)t * P.cap + bi) < dist);
+            unsigned todo = __ballot_sync(FULL, go);
+
+            // -- extend (and connect) each surviving sample, in lane order
+            while (todo) {
+                const int j = __ffs(todo) - 1;
+                todo &= todo - 1;
+                const int tj = __shfl_sync(FULL, t, j);
+                const int ni = __shfl_sync(FULL, bi, j);
+                const int iterj = __shfl_sync(FULL, iter, j);
+                const float distj = __shfl_sync(FULL, dist, j);
+#pragma unroll
+                for (int d = 0; d < D; d++) {
+                    const float v = __shfl_sync(FULL, qv[d], j);
+                    if (lane == d) W.cfg[d] = v;
+                }
+                const int o = 1 - tj;
+                float *nd_t = nodes_s + (size_t)tj * D * P.cap, *nd_o = nodes_s + (size_t)o * D * P.cap;
+                int *pr_t = par_s + (size_t)tj * P.cap;
+                float *rd_t = rad_s + (size_t)tj * P.cap;
+                const float scale = fminf(1.0f, P.range / distj);
                 if (lane < D) {
                     const float nn = __ldcg(nd_t + (size_t)lane * P.cap + ni);
                     const float c = fmaf(W.cfg[lane] - nn, scale, nn);
@@ -567,87 +620,92 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                 __syncwarp();
                 if (!warp_validate<Gen>(W, P.granularity, P.edge_order, ctx, C->work)) {
                     if (lane == 0 && P.dynamic_domain) dd_shrink(rd_t + ni, P.dd_alpha, P.dd_radius, P.dd_min_radius);
-                } else {
-                    int idx = -1;
-                    if (lane == 0) {
-                        idx = atomicAdd(&S->free_index[t], 1);
-                        if (idx >= P.max_samples || idx >= P.cap) {
-                            finish_attempt(P, S, q, idx >= P.max_samples ? 0 : PRRTC_ENOMEM);
-                            idx = -1;
-                        } else {
-                            pr_t[idx] = ni;
-                            if (P.dynamic_domain) {
-                                rd_t[idx] = FLT_MAX;
-                                dd_grow(rd_t + ni, P.dd_alpha);
-                            }
+                    continue;
+                }
+                int idx = -1;
+                if (lane == 0) {
+                    idx = atomicAdd(&S->free_index[tj], 1);
+                    if (idx >= P.max_samples || idx >= P.cap) {
+                        finish_attempt(P, S, q, idx >= P.max_samples ? 0 : PRRTC_ENOMEM);
+                        idx = -1;
+                    } else {
+                        pr_t[idx] = ni;
+                        if (P.dynamic_domain) {
+                            rd_t[idx] = FLT_MAX;
+                            dd_grow(rd_t + ni, P.dd_alpha);
                         }
-                    }
-                    idx = __shfl_sync(FULL, idx, 0);
-                    if (idx >= 0) {
-                        if (lane < D) nd_t[(size_t)lane * P.cap + idx] = W.cfg[lane];
-                        __threadfence();
-                        __syncwarp();
-                        // connect toward the other tree (pRRTC.cu:478-551)
-#pragma unroll
-                        for (int d = 0; d < D; d++) qv[d] = W.cfg[d];
-                        int oi;
-                        const int cnt_o = vload(&S->free_index[o]);
-                        warp_nn<D>(nd_o, P.cap, cnt_o, qv, dsq, oi);
-                        if (lane == 0) atomicAdd(&C->nn_nodes, (unsigned long long)min(cnt_o, P.cap));
-                        const unsigned n_ext = (unsigned)ceilf(sqrtf(dsq) / P.range);
-                        if (lane < D) W.vec[lane] = (__ldcg(nd_o + (size_t)lane * P.cap + oi) - W.cfg[lane]) / (float)n_ext;
-                        __syncwarp();
-                        unsigned i_ext = 0;
-                        int parent = idx;
-                        while (i_ext < n_ext) {
-                            if (lane < D) {
-                                const float a = W.cfg[lane];
-                                const float b = a + W.vec[lane];
-                                W.next[lane] = b;
-                                W.from[lane] = a;
-                                W.step[lane] = __fdiv_rn(__fsub_rn(b, a), fg);
-                            }
-                            __syncwarp();
-                            if (!warp_validate<Gen>(W, P.granularity, P.edge_order, ctx, C->work)) break;
-                            int idx2 = -1;
-                            if (lane == 0) {
-                                idx2 = atomicAdd(&S->free_index[t], 1);
-                                if (idx2 >= P.max_samples || idx2 >= P.cap) {
-                                    finish_attempt(P, S, q, idx2 >= P.max_samples ? 0 : PRRTC_ENOMEM);
-                                    idx2 = -1;
-                                } else {
-                                    pr_t[idx2] = parent;
-                                    rd_t[idx2] = FLT_MAX;
-                                }
-                            }
-                            idx2 = __shfl_sync(FULL, idx2, 0);
-                            if (idx2 < 0) {
-                                parent = -1;
-                                break;
-                            }
-                            if (lane < D) {
-                                W.cfg[lane] = W.next[lane];
-                                nd_t[(size_t)lane * P.cap + idx2] = W.next[lane];
-                            }
-                            __threadfence();
-                            __syncwarp();
-                            parent = idx2;
-                            i_ext++;
-                        }
-                        if (i_ext == n_ext && parent >= 0 && lane == 0) {
-                            // connected: end the attempt, then the first attempt to
-                            // win the query traces the path
-                            if (atomicCAS(&S->state, SLOT_RUNNING, SLOT_DONE) == SLOT_RUNNING) {
-                                atomicSub(&P.qstate[q].live, 1);
-                                if (atomicCAS(&P.qstate[q].state, 1, 2) == 1) {
-                                    __threadfence();
-                                    batch_trace<D>(P, S, slot, q, t, parent, oi, iter);
-                                }
-                            }
-                        }
-                        __syncwarp();
                     }
                 }
+                idx = __shfl_sync(FULL, idx, 0);
+                if (idx < 0) break;
+                if (lane < D) nd_t[(size_t)lane * P.cap + idx] = W.cfg[lane];
+                __threadfence();
+                __syncwarp();
+                // connect toward the other tree (pRRTC.cu:478-551)
+                float cq[D];
+#pragma unroll
+                for (int d = 0; d < D; d++) cq[d] = W.cfg[d];
+                float dsq;
+                int oi;
+                const int cnt_o = vload(&S->free_index[o]);
+                warp_nn<D>(nd_o, P.cap, cnt_o, cq, dsq, oi);
+                nn_visits += (unsigned long long)min(cnt_o, P.cap);
+                const unsigned n_ext = (unsigned)ceilf(sqrtf(dsq) / P.range);
+                if (lane < D) W.vec[lane] = (__ldcg(nd_o + (size_t)lane * P.cap + oi) - W.cfg[lane]) / (float)n_ext;
+                __syncwarp();
+                unsigned i_ext = 0;
+                int parent = idx;
+                while (i_ext < n_ext) {
+                    if (lane < D) {
+                        const float a = W.cfg[lane];
+                        const float b = a + W.vec[lane];
+                        W.next[lane] = b;
+                        W.from[lane] = a;
+                        W.step[lane] = __fdiv_rn(__fsub_rn(b, a), fg);
+                    }
+                    __syncwarp();
+                    if (!warp_validate<Gen>(W, P.granularity, P.edge_order, ctx, C->work)) break;
+                    int idx2 = -1;
+                    if (lane == 0) {
+                        idx2 = atomicAdd(&S->free_index[tj], 1);
+                        if (idx2 >= P.max_samples || idx2 >= P.cap) {
+                            finish_attempt(P, S, q, idx2 >= P.max_samples ? 0 : PRRTC_ENOMEM);
+                            idx2 = -1;
+                        } else {
+                            pr_t[idx2] = parent;
+                            rd_t[idx2] = FLT_MAX;
+                        }
+                    }
+                    idx2 = __shfl_sync(FULL, idx2, 0);
+                    if (idx2 < 0) {
+                        parent = -1;
+                        break;
+                    }
+                    if (lane < D) {
+                        W.cfg[lane] = W.next[lane];
+                        nd_t[(size_t)lane * P.cap + idx2] = W.next[lane];
+                    }
+                    __threadfence();
+                    __syncwarp();
+                    parent = idx2;
+                    i_ext++;
+                }
+                if (i_ext == n_ext && parent >= 0 && lane == 0) {
+                    // connected: end the attempt, then the first attempt to
+                    // win the query traces the path
+                    if (atomicCAS(&S->state, SLOT_RUNNING, SLOT_DONE) == SLOT_RUNNING) {
+                        atomicSub(&P.qstate[q].live, 1);
+                        if (atomicCAS(&P.qstate[q].state, 1, 2) == 1) {
+                            __threadfence();
+                            batch_trace<D>(P, S, slot, q, tj, parent, oi, iterj);
+                        }
+                    }
+                }
+                __syncwarp();
+                // stop once the attempt has ended (solved here, or elsewhere)
+                int ended = 0;
+                if (lane == 0) ended = vload(&S->state) != SLOT_RUNNING;
+                if (__shfl_sync(FULL, ended, 0)) break;
             }
         }
         // ---- leave an ended slot
