@@ -168,6 +168,27 @@ prrtc_status prrtc_validate_configs(prrtc_ctx *ctx, prrtc_robot robot, const prr
 prrtc_status prrtc_validate_edges(prrtc_ctx *ctx, prrtc_robot robot, const prrtc_env *env,
                                   const float *a, const float *b, int64_t n, int granularity,
                                   uint8_t *out_free);
+/*
+ * prrtc_validate_configs without allocating anything (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc or cudaFree: a control
+ * loop with a hard deadline (those calls can synchronise the device), a
+ * process whose device memory belongs to another runtime's pool, or code with
+ * a fixed memory budget.  No context is needed; verdicts are the same as
+ * prrtc_validate_configs'.
+ *   env        host arrays; at most PRRTC_MAX_ENV_FLOATS packed floats, else
+ *              PRRTC_EINVAL (the limit of the library's fixed device array)
+ *   q, out_free  device memory of the current device ([n][dof] floats, n bytes)
+ *   stream     cudaStream_t to run on (NULL: the default stream); the call
+ *              returns once the work is queued
+ * The library keeps one fixed array of PRRTC_MAX_ENV_FLOATS floats plus two
+ * counters on every GPU that loads it, for the life of the process.  Every
+ * call on a device shares it, so calls whose GPU work overlaps (other
+ * streams, other threads) race: serialise them.  The first call on a device
+ * looks up the array's address with that device current; make it before any
+ * stream capture.
+ */
+prrtc_status prrtc_validate_configs_noalloc(prrtc_robot robot, const prrtc_env_desc *env, const float *q,
+                                            int64_t n, uint8_t *out_free, void *stream);
 /* World centre and radius of every model sphere: out is [n][num_spheres][4]. */
 prrtc_status prrtc_fk_spheres(prrtc_ctx *ctx, prrtc_robot robot, const float *q, int64_t n,
                               float *out);
