@@ -297,7 +297,9 @@ def ours(args, rank, world):
         "e2e": {"value": e2e_solved / e2e_t, "unit": "queries/s", "h2d_bytes_per_step": h2d_bytes(qs) // args.steps,
                 "d2h_bytes_per_step": d2h // args.steps},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak,
+                     "traffic": (lambda b: b * len(qs) if b else None)(profiled_dram_bytes_per_query(args.workload)),
+                     "traffic_source": "ncu capture of 256 queries (profiles/), scaled by queries processed",
                      "peak_source": "measured FP32 FMA chain kernel on this GPU (prrtc_measure_fp32_peak)",
                      "nn_scan_bytes_per_s": nn_bytes / (st["kernel_ns"] * 1e-9)},
         "cpu_baseline": {"value": cs / cdt, "unit": "queries/s", "cores": threads, "kind": "port",
@@ -306,6 +308,17 @@ def ours(args, rank, world):
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
+
+
+def profiled_dram_bytes_per_query(workload: str):
+    """DRAM bytes per query of k_rrtc_batch from the committed ncu summary of a
+    smaller case of this workload (traffic scales with the queries processed)."""
+    import re
+    f = ROOT / "profiles" / f"k_rrtc_batch_{workload}.md"
+    if not f.exists():
+        return None
+    m = re.search(r"dram_bytes_per_query \| (\d+)", f.read_text())
+    return int(m.group(1)) if m else None
 
 
 def plan_dof(robot):
