@@ -285,6 +285,45 @@ prrtc_status prrtc_batch_free(prrtc_ctx *ctx, prrtc_batch *batch);
 prrtc_status prrtc_solve_batch(prrtc_ctx *ctx, prrtc_robot robot, const prrtc_query *queries, int n,
                                const prrtc_batch_settings *settings, prrtc_result *results);
 
+/* ---- differentiable clearance (no reference counterpart: pRRTC returns raw
+ * RRT-Connect paths, pRRTC.cu:568-602, and never post-processes them) ------
+ *
+ * Cost of one configuration, margin m (metres):
+ *   C(q) = 1/2 sum over env leaf spheres x obstacles of max(0, m - sd)^2
+ *        + 1/2 sum over self-collision leaf pairs of max(0, m - sd)^2
+ * sd = signed distance (negative inside; true box distance, interior
+ * included).  The leaf spheres and pairs are those the checker tests, so
+ * C(q) = 0 means every leaf test of fkcc<Robot> clears by at least m. */
+
+/* Cost and joint gradient of every waypoint of n_paths paths, path i in
+ * envs[i].  q: [n_paths][waypoints][dof]; cost: [n_paths][waypoints];
+ * grad: [n_paths][waypoints][dof] = dC/dq.  Host or device pointers.  The
+ * gradient is a hand-written adjoint that recomputes forward kinematics. */
+prrtc_status prrtc_path_cost_grad(prrtc_ctx *ctx, prrtc_robot robot, const prrtc_env *const *envs, int n_paths,
+                                  int waypoints, const float *q, float margin, float *cost, float *grad);
+
+typedef struct prrtc_smooth_settings {
+    float margin;          /* hinge margin, metres (0.02) */
+    int steps;             /* gradient steps (50) */
+    float step;            /* step size (0.05) */
+    float cost_weight;     /* weight of dC/dq (100) */
+    float smooth_weight;   /* weight of the discrete path Laplacian (1) */
+    int granularity;       /* checker points per edge for the final judgement (128) */
+} prrtc_smooth_settings;
+void prrtc_smooth_settings_default(prrtc_smooth_settings *s);
+
+/* Smooths paths in place: `steps` iterations of
+ *   q_w -= step * (cost_weight * dC/dq(q_w) + smooth_weight * (2 q_w - q_{w-1} - q_{w+1}))
+ * on the interior waypoints (end points fixed, joint limits clamped), then
+ * checks every edge with the collision checker at `granularity` points
+ * (a + k ((b - a) / g), k = 1..g).  A path is written back only if all its
+ * points are free: accepted[i] = 1; otherwise it is left exactly as given
+ * and accepted[i] = 0.  2 <= waypoints <= 256.  cost_before / cost_after
+ * (optional) receive each path's summed cost before and after. */
+prrtc_status prrtc_smooth_paths(prrtc_ctx *ctx, prrtc_robot robot, const prrtc_env *const *envs, int n_paths,
+                                int waypoints, float *q, const prrtc_smooth_settings *settings, uint8_t *accepted,
+                                float *cost_before, float *cost_after);
+
 #ifdef __cplusplus
 }
 #endif

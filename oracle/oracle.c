@@ -457,6 +457,155 @@ int oracle_clearance(int robot, const float *qf, long n, const oracle_env *e, do
     return 0;
 }
 
+/* ------------------------------------------ float64 clearance cost + gradient */
+
+/* Adds 1/2 max(0, m - sd)^2 and its gradient in the centre (-phi * dsd/dc). */
+static void hinge64(double sd, const double *gsd, double m, double *cost, double *g)
+{
+    const double phi = m - sd;
+    if (phi <= 0) return;
+    *cost += 0.5 * phi * phi;
+    for (int k = 0; k < 3; k++) g[k] -= phi * gsd[k];
+}
+
+static void point64(const double *d, double rsum, double m, double *cost, double *g)
+{
+    const double len = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const double u[3] = {len > 0 ? d[0] / len : 0, len > 0 ? d[1] / len : 0, len > 0 ? d[2] / len : 0};
+    hinge64(len - rsum, u, m, cost, g);
+}
+
+/* Signed distance of a sphere to a box: centre ce, unit axes ax[3][3], half extents h. */
+static void box64(const double *p, double r, const double *ce, const double ax[3][3], const double *h, double m,
+                  double *cost, double *g)
+{
+    double u[3], q[3], s[3];
+    for (int a = 0; a < 3; a++) {
+        u[a] = ax[a][0] * (p[0] - ce[0]) + ax[a][1] * (p[1] - ce[1]) + ax[a][2] * (p[2] - ce[2]);
+        s[a] = u[a] < 0 ? -1.0 : 1.0;
+        q[a] = fabs(u[a]) - h[a];
+    }
+    double sd, gsd[3] = {0, 0, 0};
+    if (q[0] > 0 || q[1] > 0 || q[2] > 0) {
+        double o2 = 0, w[3];
+        for (int a = 0; a < 3; a++) {
+            w[a] = (q[a] > 0 ? q[a] : 0) * s[a];
+            o2 += w[a] * w[a];
+        }
+        const double o = sqrt(o2);
+        sd = o - r;
+        for (int a = 0; a < 3; a++)
+            for (int k = 0; k < 3; k++) gsd[k] += w[a] * ax[a][k] / o;
+    } else {
+        int a = 0;
+        if (q[1] > q[a]) a = 1;
+        if (q[2] > q[a]) a = 2;
+        sd = q[a] - r;
+        for (int k = 0; k < 3; k++) gsd[k] = s[a] * ax[a][k];
+    }
+    hinge64(sd, gsd, m, cost, g);
+}
+
+static void env_cost64(const oracle_env *e, const double *p, double r, double m, double *cost, double *g)
+{
+    for (int i = 0; i < e->ns; i++) {
+        const float *s = e->spheres + 4 * i;
+        const double d[3] = {p[0] - s[0], p[1] - s[1], p[2] - s[2]};
+        point64(d, r + s[3], m, cost, g);
+    }
+    for (int k = 0; k < 2; k++) {
+        const float *base = k ? e->zcapsules : e->capsules;
+        const int n = k ? e->nzc : e->nc;
+        for (int i = 0; i < n; i++) {
+            const float *c = base + 8 * i;   /* p1 (0..2), v (3..5), r (6), 1/|v|^2 (7) */
+            double t = k ? (p[2] - c[2]) * c[5] * (double)c[7]
+                         : ((p[0] - c[0]) * c[3] + (p[1] - c[1]) * c[4] + (p[2] - c[2]) * c[5]) * (double)c[7];
+            t = t < 0 ? 0 : (t > 1 ? 1 : t);
+            const double d[3] = {p[0] - (k ? c[0] : c[0] + c[3] * t), p[1] - (k ? c[1] : c[1] + c[4] * t),
+                                 p[2] - (c[2] + c[5] * t)};
+            point64(d, r + c[6], m, cost, g);
+        }
+    }
+    for (int k = 0; k < 2; k++) {
+        const float *base = k ? e->zcuboids : e->cuboids;
+        const int n = k ? e->nzb : e->ncb;
+        for (int i = 0; i < n; i++) {
+            const float *c = base + 15 * i;  /* centre (0..2), axes (3..11), half extents (12..14) */
+            const double ce[3] = {c[0], c[1], c[2]}, h[3] = {c[12], c[13], c[14]};
+            double ax[3][3];
+            if (k) {
+                const double z[3][3] = {{c[3], c[4], 0}, {c[6], c[7], 0}, {0, 0, 1}};
+                memcpy(ax, z, sizeof ax);
+            } else {
+                for (int a = 0; a < 3; a++)
+                    for (int j = 0; j < 3; j++) ax[a][j] = c[3 + 3 * a + j];
+            }
+            box64(p, r, ce, ax, h, m, cost, g);
+        }
+    }
+}
+
+/* grad[q] += g . dc/dq over every joint that moves the sphere on `frame`. */
+static void jacobian_t(const robot_t *R, const frames_t *fr, const int *pos, int frame, const double *c,
+                       const double *g, double *grad)
+{
+    for (int f = frame; f >= 0; f = R->joints[pos[f]].parent) {
+        const prrtc_joint_def *J = &R->joints[pos[f]];
+        const double *T = fr->T[f];
+        const double z[3] = {T[2], T[6], T[10]};
+        if (J->revolute) {
+            const double v[3] = {c[0] - T[3], c[1] - T[7], c[2] - T[11]};
+            const double dc[3] = {z[1] * v[2] - z[2] * v[1], z[2] * v[0] - z[0] * v[2], z[0] * v[1] - z[1] * v[0]};
+            grad[f] += g[0] * dc[0] + g[1] * dc[1] + g[2] * dc[2];
+        } else {
+            grad[f] += g[0] * z[0] + g[1] * z[1] + g[2] * z[2];
+        }
+    }
+}
+
+int oracle_cost_grad(int robot, const double *q, long n, const oracle_env *e, double margin, double *cost,
+                     double *grad)
+{
+    const robot_t *R = robot_get(robot);
+    if (!R || !e) return -1;
+    int pos[14];
+    for (int j = 0; j < R->nj; j++) pos[R->joints[j].q] = j;
+#pragma omp parallel for schedule(static, 16)
+    for (long i = 0; i < n; i++) {
+        const double *qi = q + i * R->dof;
+        double *gi = grad + i * R->dof;
+        frames_t fr;
+        fk_frames(R, qi, &fr);
+        double c[128][3];
+        for (int s = 0; s < R->ns; s++) sphere_centre(R, &fr, s, c[s]);
+        for (int d = 0; d < R->dof; d++) gi[d] = 0;
+        double C = 0;
+        for (int gr = 0; gr < R->neg; gr++) {
+            const prrtc_group_def *G = &R->env_groups[gr];
+            for (int l = 0; l < G->count; l++) {
+                const int s = R->env_leaves[G->first + l];
+                double g[3] = {0, 0, 0};
+                env_cost64(e, c[s], R->spheres[s].r, margin, &C, g);
+                jacobian_t(R, &fr, pos, R->spheres[s].frame, c[s], g, gi);
+            }
+        }
+        for (int gr = 0; gr < R->nsg; gr++) {
+            const prrtc_group_def *G = &R->self_groups[gr];
+            for (int l = 0; l < G->count; l++) {
+                const int a = R->self_pairs[G->first + l][0], b = R->self_pairs[G->first + l][1];
+                const double d[3] = {c[a][0] - c[b][0], c[a][1] - c[b][1], c[a][2] - c[b][2]};
+                double g[3] = {0, 0, 0};
+                point64(d, (double)R->spheres[a].r + R->spheres[b].r, margin, &C, g);
+                const double ng[3] = {-g[0], -g[1], -g[2]};
+                jacobian_t(R, &fr, pos, R->spheres[a].frame, c[a], g, gi);
+                jacobian_t(R, &fr, pos, R->spheres[b].frame, c[b], ng, gi);
+            }
+        }
+        cost[i] = C;
+    }
+    return 0;
+}
+
 /* ------------------------------------------------------------- the planner */
 
 typedef struct {

@@ -56,6 +56,18 @@ int oracle_check_edges(int robot, const float *a, const float *b, long n, int g,
 int oracle_clearance(int robot, const float *q, long n, const oracle_env *env, double *out);
 
 /*
+ * Float64 clearance cost and its gradient (the differentiable clearance of
+ * prrtc_path_cost_grad; no reference counterpart).  Per configuration:
+ *   C = 1/2 sum over leaf spheres x obstacles and leaf self pairs of max(0, m - sd)^2
+ * with sd the float64 signed distance (boxes: true distance, interior
+ * included).  grad[i][d] = dC/dq_d, assembled with the geometric Jacobian of
+ * each sphere centre (z_j x (c - o_j) per revolute ancestor joint j, z_j per
+ * prismatic one) -- a different route from the library's tip-to-base sweep.
+ */
+int oracle_cost_grad(int robot, const double *q, long n, const oracle_env *env, double margin, double *cost,
+                     double *grad);
+
+/*
  * RRT-Connect as pRRTC runs it (rrtc<Robot>, pRRTC.cu:305-602), with its
  * `num_new_configs` lanes emulated in round-robin order on one thread.
  * Settings are pRRTC_settings fields.  bases: [lanes][16] Halton prime bases

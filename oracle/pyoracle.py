@@ -65,6 +65,8 @@ class OracleLib:
         self.L.oracle_check.argtypes = [C.c_int, C.c_void_p, C.c_long, C.POINTER(OEnv), C.c_void_p, C.c_void_p, C.c_void_p]
         self.L.oracle_check_edges.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.POINTER(OEnv), C.c_void_p]
         self.L.oracle_clearance.argtypes = [C.c_int, C.c_void_p, C.c_long, C.POINTER(OEnv), C.c_void_p]
+        self.L.oracle_cost_grad.argtypes = [C.c_int, C.c_void_p, C.c_long, C.POINTER(OEnv), C.c_double, C.c_void_p,
+                                            C.c_void_p]
         self.L.oracle_fk_spheres.argtypes = [C.c_int, C.c_void_p, C.c_long, C.c_void_p]
         self.L.oracle_solve.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(OEnv), C.POINTER(OSettings),
                                         C.c_void_p, C.c_void_p, C.c_int, C.POINTER(OResult)]
@@ -106,6 +108,17 @@ class OracleLib:
         out = np.empty(len(q), np.float64)
         assert self.L.oracle_clearance(ROBOTS[robot], q.ctypes.data, len(q), C.byref(e.s), out.ctypes.data) == 0
         return out
+
+    def cost_grad(self, robot, env, q, margin):
+        """Float64 clearance cost [n] and gradient [n][dof] of configurations q (float64)."""
+        D = self.dof(robot)
+        q = np.ascontiguousarray(np.asarray(q, np.float64).reshape(-1, D))
+        e = _EnvRef(env)
+        cost = np.empty(len(q), np.float64)
+        grad = np.empty((len(q), D), np.float64)
+        assert self.L.oracle_cost_grad(ROBOTS[robot], q.ctypes.data, len(q), C.byref(e.s), float(margin),
+                                       cost.ctypes.data, grad.ctypes.data) == 0
+        return cost, grad
 
     def fk_spheres(self, robot, q):
         D = self.dof(robot)

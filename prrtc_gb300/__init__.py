@@ -3,6 +3,6 @@
 The product is the shared library ``libprrtc_gb300.so`` (C ABI in
 ``include/prrtc/prrtc.h``); ``api`` is its Python host mirror.
 """
-from .api import (Batch, BatchSettings, Context, EnvHandle, PlannerResult, PrrtcError, Settings, dof,  # noqa: F401
-                  num_spheres, robot_id)
+from .api import (Batch, BatchSettings, Context, EnvHandle, PlannerResult, PrrtcError, Settings,  # noqa: F401
+                  SmoothSettings, dof, num_spheres, robot_id)
 from .env import Environment  # noqa: F401

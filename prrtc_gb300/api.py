@@ -93,6 +93,20 @@ class BatchSettings(C.Structure):
             setattr(self, k, v)
 
 
+class SmoothSettings(C.Structure):
+    """prrtc_smooth_settings."""
+    _fields_ = [("margin", C.c_float), ("steps", C.c_int), ("step", C.c_float), ("cost_weight", C.c_float),
+                ("smooth_weight", C.c_float), ("granularity", C.c_int)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        lib().prrtc_smooth_settings_default(C.byref(self))
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(k)
+            setattr(self, k, v)
+
+
 class _BatchStats(C.Structure):
     _fields_ = [("kernel_ns", C.c_uint64), ("samples", C.c_int64), ("solved", C.c_int), ("blocks", C.c_int),
                 ("warps_per_block", C.c_int), ("slots", C.c_int), ("error", C.c_int), ("extra_attempts", C.c_int),
@@ -149,6 +163,10 @@ def lib():
             "prrtc_batch_stats_get": (C.c_int, [vp, vp, C.POINTER(_BatchStats)]),
             "prrtc_batch_free": (C.c_int, [vp, vp]),
             "prrtc_solve_batch": (C.c_int, [vp, C.c_int, C.POINTER(_Query), C.c_int, C.POINTER(BatchSettings), C.POINTER(_Result)]),
+            "prrtc_path_cost_grad": (C.c_int, [vp, C.c_int, C.POINTER(vp), C.c_int, C.c_int, fp, C.c_float, fp, fp]),
+            "prrtc_smooth_settings_default": (None, [C.POINTER(SmoothSettings)]),
+            "prrtc_smooth_paths": (C.c_int, [vp, C.c_int, C.POINTER(vp), C.c_int, C.c_int, fp, C.POINTER(SmoothSettings),
+                                             u8p, fp, fp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -293,6 +311,61 @@ class Context:
         po, ko = _ptr(out)
         self._check(lib().prrtc_fk_spheres(self.handle, rid, pq, n, po))
         return out
+
+    def _env_table(self, envs, n_paths: int):
+        seen = {}   # one upload per distinct environment object
+        hs = []
+        for e in (envs if isinstance(envs, (list, tuple)) else [envs] * n_paths):
+            if id(e) not in seen:
+                seen[id(e)] = self._env(e)
+            hs.append(seen[id(e)])
+        if len(hs) != n_paths:
+            raise ValueError(f"{len(hs)} environments for {n_paths} paths")
+        return (C.c_void_p * n_paths)(*[h.handle.value for h in hs]), hs
+
+    def path_cost_grad(self, robot, envs, q, margin: float = 0.02):
+        """Clearance cost [P, W] and gradient [P, W, dof] of paths q [P, W, dof]
+        (numpy or CUDA tensor); envs: one environment per path, or one for all."""
+        rid = robot_id(robot)
+        D = dof(rid)
+        dev = hasattr(q, "data_ptr")
+        q = q.contiguous() if dev else np.ascontiguousarray(np.asarray(q, np.float32))
+        P, W = q.shape[0], q.shape[1]
+        assert q.shape[2] == D
+        table, keep = self._env_table(envs, P)
+        if dev:
+            cost, grad = _empty_like_device(q, (P, W), "float32"), _empty_like_device(q, (P, W, D), "float32")
+        else:
+            cost, grad = np.empty((P, W), np.float32), np.empty((P, W, D), np.float32)
+        pq, kq = _ptr(q)
+        pc, kc = _ptr(cost)
+        pg, kg = _ptr(grad)
+        self._check(lib().prrtc_path_cost_grad(self.handle, rid, table, P, W, pq, float(margin), pc, pg))
+        return cost, grad
+
+    def smooth_paths(self, robot, envs, q, settings: SmoothSettings | None = None):
+        """Smooths paths q [P, W, dof] (numpy: a smoothed copy is returned; CUDA
+        tensor: smoothed in place).  Returns (q, accepted[P], cost_before[P],
+        cost_after[P]); rejected paths are returned unchanged."""
+        rid = robot_id(robot)
+        D = dof(rid)
+        s = settings if settings is not None else SmoothSettings()
+        dev = hasattr(q, "data_ptr")
+        q = q.contiguous() if dev else np.array(q, np.float32, copy=True, order="C")
+        P, W = q.shape[0], q.shape[1]
+        assert q.shape[2] == D
+        table, keep = self._env_table(envs, P)
+        if dev:
+            acc = _empty_like_device(q, (P,), "uint8")
+            cb, ca = _empty_like_device(q, (P,), "float32"), _empty_like_device(q, (P,), "float32")
+        else:
+            acc, cb, ca = np.empty(P, np.uint8), np.empty(P, np.float32), np.empty(P, np.float32)
+        pq, kq = _ptr(q)
+        pa, ka = _ptr(acc)
+        pb, kb = _ptr(cb)
+        pc, kc = _ptr(ca)
+        self._check(lib().prrtc_smooth_paths(self.handle, rid, table, P, W, pq, C.byref(s), pa, pb, pc))
+        return q, acc, cb, ca
 
     def batch(self, robot, queries, settings: BatchSettings | None = None, path_capacity: int = 4096) -> Batch:
         """Prepare a batch; queries are (env, start, goals) tuples or objects

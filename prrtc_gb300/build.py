@@ -20,7 +20,7 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
          f"-I{ROOT / 'include'}", f"-I{CSRC}"]
-SOURCES = ["capi.cu", "planner.cu", "batch.cu", "noalloc.cu", "robot_sphere.cu", "robot_panda.cu", "robot_fetch.cu", "robot_baxter.cu"]
+SOURCES = ["capi.cu", "planner.cu", "batch.cu", "noalloc.cu", "clearance.cu", "robot_sphere.cu", "robot_panda.cu", "robot_fetch.cu", "robot_baxter.cu"]
 
 
 def _deps() -> float:

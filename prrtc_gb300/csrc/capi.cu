@@ -188,6 +188,7 @@ prrtc_status prrtc_destroy(prrtc_ctx *ctx)
             if (b.ptr) cudaFree(b.ptr);
         c->release_planner_state();
         release_arena(c);
+        release_clearance_state(c);
         cudaFree(c->work_dev);
         cudaStreamDestroy(c->stream);
     }

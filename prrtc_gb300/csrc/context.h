@@ -46,7 +46,8 @@ inline void pack_env(const prrtc_env_desc &d, std::vector<float4> &out)
     cubs(d.z_aligned_cuboids, d.num_z_aligned_cuboids);
 }
 
-struct PlannerState;  // planner.cu
+struct PlannerState;    // planner.cu
+struct ClearanceState;  // clearance.cu
 
 struct Ctx {
     int device = 0;
@@ -67,6 +68,7 @@ struct Ctx {
     unsigned long long *work_dev = nullptr; // [2] FLOPs, configurations (prrtc_work_counters)
     float plan_pad = 0.0f;                  // prrtc_set_planning_margin
     unsigned long long budget_ns = 0;       // prrtc_set_time_budget
+    ClearanceState *clearance = nullptr;    // robot tables for the clearance cost
 
     static Ctx *of(prrtc_ctx *c) { return reinterpret_cast<Ctx *>(c); }
     prrtc_status fail(prrtc_status s, const char *fmt, ...);
@@ -80,6 +82,7 @@ struct Ctx {
 const RobotOps *robot_ops(prrtc_robot r);
 prrtc_status ensure_halton_bases(Ctx *c, int lanes);
 void release_arena(Ctx *c);
+void release_clearance_state(Ctx *c);
 
 struct Limits;
 const Limits *robot_limits(prrtc_robot r);

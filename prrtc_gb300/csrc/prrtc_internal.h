@@ -148,6 +148,8 @@ struct BatchParams {
     float scale[16], offset[16];
 };
 
+struct ClrLaunch;   // clearance_device.cuh
+
 struct RobotOps {
     int dof;
     int num_spheres;
@@ -158,6 +160,7 @@ struct RobotOps {
     cudaError_t (*solve_plain)(const PlainParams &, int threads, cudaStream_t);
     cudaError_t (*solve_batch)(const BatchParams &, int blocks, int warps_per_block, cudaStream_t);
     int (*batch_occupancy)(int warps_per_block);   // resident blocks per SM
+    cudaError_t (*smooth_paths)(const ClrLaunch &, size_t env_bytes, cudaStream_t);
 };
 
 // Shuffled Halton prime bases per sampling lane, as the reference seeds them

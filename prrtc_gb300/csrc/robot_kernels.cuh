@@ -2,6 +2,7 @@
 // robot's generated checker; GEN names the generated namespace.
 #pragma once
 
+#include "clearance_kernel.cuh"
 #include "device_common.cuh"
 #include "planner_device.cuh"
 #include "prrtc_internal.h"
@@ -390,6 +391,16 @@ struct RobotKernels {
         }
         return n;
     }
+    static cudaError_t smooth_paths(const ClrLaunch &P, size_t env_bytes, cudaStream_t st)
+    {
+        if (P.n_paths <= 0) return cudaSuccess;
+        const size_t smem = env_bytes + 2 * sizeof(float) * (size_t)P.waypoints * Gen::kDof;
+        cudaError_t e = cudaFuncSetAttribute(k_smooth_paths<Gen>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        const int threads = P.waypoints <= 64 ? 64 : 128;
+        k_smooth_paths<Gen><<<P.n_paths, threads, smem, st>>>(P);
+        return cudaGetLastError();
+    }
     static RobotOps ops(int dof_check)
     {
         RobotOps o{};
@@ -401,6 +412,7 @@ struct RobotKernels {
         o.solve_plain = &solve_plain;
         o.solve_batch = &solve_batch;
         o.batch_occupancy = &batch_occupancy;
+        o.smooth_paths = &smooth_paths;
         (void)dof_check;
         return o;
     }
