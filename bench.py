@@ -276,10 +276,22 @@ def ours(args, rank, world):
     threads = os.cpu_count() or 1
     cs, cdt, _ = cpu_planner(robot, qs[:ns_cpu], plan, threads)
 
+    # ---- the other configurations, one launch each
+    others, baxter = {}, None
+    if args.others:
+        for name, cnt in OTHER_WORKLOADS:
+            if name == args.workload:
+                continue
+            info, run = workload_run(ctx, O, name, cnt)
+            others[f"{name}_{cnt}"] = info
+            if name == "baxter_mixed":
+                baxter = run
+            log(name, json.dumps(info))
+
     # ---- differentiable clearance: smoothing of this run's paths (and Baxter's)
     clearance = None
     if args.clearance and robot == "panda":
-        clearance = clearance_leg(ctx, O, qs, results, envs)
+        clearance = clearance_leg(ctx, O, qs, results, envs, baxter)
 
     single_med = statistics.median(single_ms)
     line = {
@@ -311,6 +323,7 @@ def ours(args, rank, world):
                          "sample": f"first {ns_cpu} of the {len(qs)} queries, oracle RRT-Connect restatement"},
         "gpu_launches": launches,
         "clocks": clk.summary(),
+        "other_workloads": others or None,
         "clearance": clearance,
     }
     print(json.dumps(line), flush=True)
@@ -353,23 +366,51 @@ def resampled(qs, results, envs, n):
     return E, H, np.stack(P)
 
 
-def clearance_leg(ctx, O, qs, results, envs):
+def clearance_leg(ctx, O, qs, results, envs, baxter):
     """Differentiable clearance: 4096 Panda paths of this run and 1024 Baxter
     paths (tabletop and shelf scenes) resampled to 64 waypoints, margin 0.02 m,
     50 smoothing steps, the checker as judge."""
-    from prrtc_gb300 import BatchSettings, autotune, workloads
     out = {"config": "paths resampled to 64 waypoints (planner vertices kept), margin 0.02 m, 50 steps, "
                      "judged at 128 points per edge by the robot's checker, then re-checked by the oracle"}
     E, H, P = resampled(qs, results, envs, 4096)
     out["panda"] = smooth_and_judge(ctx, O, "panda", E, H, P)
-    bq = workloads.make("baxter_mixed", 1024)
-    be = [ctx.upload_env(q.env) for q in bq]
-    bs = BatchSettings(settings_for("baxter_mixed"), use_graph=1, margin=MARGIN, time_budget_ns=GPU_BUDGET_NS,
-                       **autotune.load("baxter", "baxter_mixed"))
-    bres = ctx.solve_batch("baxter", [(e, q.start, q.goal) for e, q in zip(be, bq)], bs, path_capacity=2048)
-    E, H, P = resampled(bq, bres, be, 1024)
-    out["baxter"] = smooth_and_judge(ctx, O, "baxter", E, H, P)
+    if baxter is not None:
+        E, H, P = resampled(*baxter, 1024)
+        out["baxter"] = smooth_and_judge(ctx, O, "baxter", E, H, P)
     return out
+
+
+# the other configurations: one launch of n queries each (after one warm-up launch)
+OTHER_WORKLOADS = [("panda_tabletop", 1024), ("fetch_mixed", 256), ("baxter_mixed", 1024)]
+
+
+def workload_run(ctx, O, name, n):
+    """queries/s, p50/p99 and edge validations/s of one batched launch of
+    workload `name`, every path revalidated by the oracle."""
+    from prrtc_gb300 import BatchSettings, autotune, workloads
+    robot = workloads.WORKLOADS[name][0]
+    qs = workloads.make(name, n)
+    envs = [ctx.upload_env(q.env) for q in qs]
+    plan = settings_for(name)
+    b = ctx.batch(robot, [(e, q.start, q.goal) for e, q in zip(envs, qs)],
+                  BatchSettings(plan, use_graph=1, margin=MARGIN, time_budget_ns=GPU_BUDGET_NS,
+                                **autotune.load(robot, name)), path_capacity=2048)
+    b.run()
+    b.run()
+    st, res = b.stats(), b.results()
+    b.free()
+    t = st["kernel_ns"] * 1e-9
+    solved = sum(r.solved for r in res)
+    g = plan.granularity
+    bad = sum(1 for q, r in zip(qs, res) if r.solved and not O.check_edges(robot, q.env, r.path[:-1], r.path[1:], g).all())
+    lat = [r.kernel_ns / 1e6 for r in res if r.solved]
+    info = {"queries": n, "settings": WORKLOAD_SETTINGS[name], "queries_per_s": solved / t, "ms": t * 1e3,
+            "success_rate": solved / n, "revalidated": f"{solved - bad}/{solved}",
+            "p50_solve_ms": statistics.median(lat) if lat else None,
+            "p99_solve_ms": float(np.percentile(lat, 99)) if lat else None,
+            "edge_validations_per_s": st["configs_checked"] / g / t,
+            "fp32_tflops": st["flops"] / t / 1e12}
+    return info, (qs, res, envs)
 
 
 def profiled_dram_bytes_per_query(workload: str):
@@ -397,6 +438,8 @@ def main():
     ap.add_argument("--queries", type=int, default=1024)
     ap.add_argument("--no-clearance", dest="clearance", action="store_false",
                     help="skip the path-smoothing measurement")
+    ap.add_argument("--no-others", dest="others", action="store_false",
+                    help="skip the one-launch runs of the other configurations")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
