@@ -249,6 +249,10 @@ typedef struct prrtc_batch_settings {
     int use_graph;                   /* replay each run as a captured CUDA graph */
     float margin;                    /* sphere inflation while planning, metres (>= 0) */
     uint64_t time_budget_ns;         /* 0: none */
+    int admission;                   /* order queries start in when slots are fewer than queries:
+                                        0 tightest first (smallest clearance of start or goal to an
+                                        obstacle, computed on the GPU at create: the hard queries
+                                        start early and no longer set the batch's end); 1 as given */
 } prrtc_batch_settings;
 
 typedef struct prrtc_batch prrtc_batch;

@@ -196,6 +196,8 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     off = align256(off + std::max<size_t>(1, envs.size()) * sizeof(float4));
     const size_t o_desc = off;
     off = align256(off + n * sizeof(BatchQueryDesc));
+    const size_t o_order = off;
+    off = align256(off + n * sizeof(int));
     const size_t o_qstate = off;
     off = align256(off + n * sizeof(QueryState));
     const size_t o_slots = off;
@@ -226,7 +228,27 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
         prrtc_batch_free(ctx, b);
         return s;
     }
+    // admission order: tightest start/goal clearance first (longest expected
+    // solve first), so the hard queries do not start last and end the batch
+    int *order_dev = nullptr;
+    if (settings->admission == 0 && n > 1) {
+        std::vector<float> score(n);
+        if ((s = query_clearance(c, robot, reinterpret_cast<const BatchQueryDesc *>(base + o_desc),
+                                 reinterpret_cast<const float *>(base + o_cfg), n, score.data()))) {
+            prrtc_batch_free(ctx, b);
+            return s;
+        }
+        std::vector<int> order(n);
+        for (int i = 0; i < n; i++) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return score[x] < score[y]; });
+        order_dev = reinterpret_cast<int *>(base + o_order);
+        if ((s = c->cuda(cudaMemcpy(order_dev, order.data(), n * sizeof(int), cudaMemcpyHostToDevice), "batch order"))) {
+            prrtc_batch_free(ctx, b);
+            return s;
+        }
+    }
     BatchParams &P = b->P;
+    P.order = order_dev;
     P.max_samples = S.max_samples;
     P.max_iters = S.max_iters;
     P.lanes = b->lanes;

@@ -307,6 +307,7 @@ __device__ bool batch_leave(const BatchParams &P, int s, bool allow_admit)
             if (qa >= P.num_queries) {
                 qa = -1;
             } else {
+                if (P.order) qa = P.order[qa];
                 att = 0;
                 open_query(P, qa);
             }
@@ -393,8 +394,9 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                     const int st = vload(&S->state);
                     if (st == SLOT_FREE && pending) {
                         if (atomicCAS(&S->state, SLOT_FREE, SLOT_BUSY) != SLOT_FREE) continue;
-                        const int qa = atomicAdd(&C->admit_next, 1);
+                        int qa = atomicAdd(&C->admit_next, 1);
                         if (qa < P.num_queries) {
+                            if (P.order) qa = P.order[qa];
                             open_query(P, qa);
                             atomicAdd(&S->workers, 1);
                             found = s;

@@ -33,6 +33,19 @@ __global__ void __launch_bounds__(64) k_path_cost_grad(ClrModel M, const ClrEnv 
     for (int d = 0; d < M.dof; d++) grad[row * M.dof + d] = g[d];
 }
 
+// One thread per query: the smallest clearance of its start and goals.
+__global__ void __launch_bounds__(64) k_query_clearance(ClrModel M, const BatchQueryDesc *__restrict__ queries,
+                                                       const float *__restrict__ cfg, int n, float *__restrict__ score)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const BatchQueryDesc d = queries[i];
+    const ClrEnv e{d.env, d.env_n};
+    float best = 3.4e38f;
+    for (int c = 0; c <= d.num_goals; c++) best = fminf(best, clr::min_clearance(M, e, cfg + d.cfg_off + c * M.dof));
+    score[i] = best;
+}
+
 namespace {
 
 size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -55,10 +68,9 @@ void release_clearance_state(Ctx *c)
     c->clearance = nullptr;
 }
 
-// The robot's tables on the device (uploaded on first use) and the per-path
-// obstacle table of this call.  Caller holds c->mu with the device current.
-static prrtc_status prepare(Ctx *c, prrtc_robot robot, const prrtc_env *const *envs, int n_paths, ClrModel *model,
-                            int *max_records)
+// The robot's tables on the device, uploaded on first use.  Caller holds
+// c->mu with the device current.
+static prrtc_status model_on_device(Ctx *c, prrtc_robot robot, ClrModel *model)
 {
     if (!c->clearance) c->clearance = new ClearanceState();
     ClearanceState *cs = c->clearance;
@@ -103,6 +115,17 @@ static prrtc_status prepare(Ctx *c, prrtc_robot robot, const prrtc_env *const *e
         cs->tables[robot] = d;
     }
     *model = cs->model[robot];
+    return PRRTC_OK;
+}
+
+// The robot's tables and the per-path obstacle table of this call.  Caller
+// holds c->mu with the device current.
+static prrtc_status prepare(Ctx *c, prrtc_robot robot, const prrtc_env *const *envs, int n_paths, ClrModel *model,
+                            int *max_records)
+{
+    prrtc_status s = model_on_device(c, robot, model);
+    if (s) return s;
+    ClearanceState *cs = c->clearance;
     std::vector<ClrEnv> table(n_paths);
     int mr = 0;
     for (int i = 0; i < n_paths; i++) {
@@ -112,8 +135,7 @@ static prrtc_status prepare(Ctx *c, prrtc_robot robot, const prrtc_env *const *e
         mr = std::max(mr, e->counts.records());
     }
     // earlier work on the context's stream may still read the old table
-    prrtc_status s = c->cuda(cudaStreamSynchronize(c->stream), "clearance: stream");
-    if (s) return s;
+    if ((s = c->cuda(cudaStreamSynchronize(c->stream), "clearance: stream"))) return s;
     if (cs->envs_cap < n_paths) {
         cudaFree(cs->envs);
         cs->envs = nullptr;
@@ -128,6 +150,23 @@ static prrtc_status prepare(Ctx *c, prrtc_robot robot, const prrtc_env *const *e
     // `table` is pageable and local: a synchronous copy
     return c->cuda(cudaMemcpy(cs->envs, table.data(), sizeof(ClrEnv) * n_paths, cudaMemcpyHostToDevice),
                    "clearance: obstacle table");
+}
+
+prrtc_status query_clearance(Ctx *c, prrtc_robot robot, const BatchQueryDesc *queries, const float *cfg_pool, int n,
+                             float *score)
+{
+    ClrModel M;
+    prrtc_status s = model_on_device(c, robot, &M);
+    if (s) return s;
+    float *d = static_cast<float *>(c->scratch(3, (size_t)n * sizeof(float)));
+    if (!d) return c->fail(PRRTC_ENOMEM, "query_clearance: scratch");
+    k_query_clearance<<<(n + 63) / 64, 64, 0, c->stream>>>(M, queries, cfg_pool, n, d);
+    if ((s = c->cuda(cudaGetLastError(), "query_clearance: launch"))) return s;
+    c->launches++;
+    if ((s = c->cuda(cudaMemcpyAsync(score, d, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, c->stream),
+                     "query_clearance: copy")))
+        return s;
+    return c->cuda(cudaStreamSynchronize(c->stream), "query_clearance");
 }
 
 }  // namespace prrtc

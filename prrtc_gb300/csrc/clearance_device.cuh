@@ -289,6 +289,47 @@ static __host__ __device__ double3 env_force(const ClrEnv e, const double (*T)[1
     return g;
 }
 
+// Smallest float32 signed distance of sphere (cf, r) to any obstacle.
+static __host__ __device__ float env_min_sd(const ClrEnv e, float3 cf, float r)
+{
+    float best = 3.4e38f;
+    const float4 *p = e.rec;
+    for (int i = 0; i < e.n.ns; i++) best = fminf(best, sd_point_f(sub(cf, f3(p[i].x, p[i].y, p[i].z)), r + p[i].w));
+    p += e.n.ns;
+    for (int k = 0; k < 2; k++) {
+        const int n = k ? e.n.nzc : e.n.nc;
+        for (int i = 0; i < n; i++) best = fminf(best, sd_capsule_f(cf, r, p[2 * i], p[2 * i + 1], k));
+        p += 2 * n;
+    }
+    for (int k = 0; k < 2; k++) {
+        const int n = k ? e.n.nzb : e.n.ncb;
+        for (int i = 0; i < n; i++) {
+            const float4 c0 = p[4 * i], c1 = p[4 * i + 1], c2 = p[4 * i + 2], c3 = p[4 * i + 3];
+            best = fminf(best, sd_box_f(cf, r, f3(c0.x, c0.y, c0.z), f3(c1.x, c1.y, k ? 0.0f : c1.z),
+                                        f3(c2.x, c2.y, k ? 0.0f : c2.z), k ? f3(0.0f, 0.0f, 1.0f) : f3(c3.x, c3.y, c3.z),
+                                        f3(c0.w, c1.w, c2.w)));
+        }
+        p += 4 * n;
+    }
+    return best;
+}
+
+// Smallest signed distance of configuration q's env leaf spheres to the obstacles.
+static __host__ __device__ float min_clearance(const ClrModel &M, const ClrEnv e, const float *q)
+{
+    double T[kClrMaxJoints][12];
+    float Tf[kClrMaxJoints][12];
+    fk(M, q, T);
+    for (int j = 0; j < M.nj; j++)
+        for (int k = 0; k < 12; k++) Tf[j][k] = (float)T[j][k];
+    float best = 3.4e38f;
+    for (int i = 0; i < M.n_leaf; i++) {
+        const float4 l = M.leaf[i];
+        best = fminf(best, env_min_sd(e, place(Tf, M.leaf_joint[i], l), l.w));
+    }
+    return best;
+}
+
 // Cost of configuration q (dof floats); grad[d] = scale * dC/dq[d] for every dof.
 static __host__ __device__ __noinline__ float cost_grad(const ClrModel &M, const ClrEnv e, const float *q, float mf,
                                                         float scale_f, float *grad)

@@ -136,6 +136,7 @@ struct BatchParams {
     unsigned long long restart_after_ns;   // a query may get its k-th extra attempt after k x this
     const float *cfg_pool;
     const BatchQueryDesc *queries;
+    const int *order;    // admission order (query ids), null: index order
     QueryState *qstate;
     SlotState *slots;
     BatchOut *out;
@@ -149,6 +150,12 @@ struct BatchParams {
 };
 
 struct ClrLaunch;   // clearance_device.cuh
+struct Ctx;         // context.h
+
+// score[i] = smallest clearance (metres, float32 screen) of query i's start or
+// goals to its obstacles, over the robot's env leaf spheres (clearance.cu).
+prrtc_status query_clearance(Ctx *c, prrtc_robot robot, const BatchQueryDesc *queries, const float *cfg_pool, int n,
+                             float *score);
 
 struct RobotOps {
     int dof;
