@@ -101,32 +101,54 @@ constexpr int kFlopSphere = 11, kFlopCapsule = 26, kFlopZCapsule = 16, kFlopCubo
 // (sphere_environment_in_collision, utils.cuh:211-242).  Not inlined: every
 // generated call site shares one copy of the obstacle loops.  Returns
 // 2 * (FLOPs of the tests executed) + (1 if hit).
+//
+// Spheres, capsules and cuboids are tested two at a time (independent
+// dependency chains, one branch); on a hit the count stops at the first
+// hitting test, so verdicts and counts are the reference's, in its order.
 static __device__ __noinline__ int env_hit(const EnvView e, float x, float y, float z, float r)
 {
     const float4 *p = e.rec;
-    int w = 0;
-    for (int i = 0; i < e.n.ns; i++) {
+    int w = 0, i = 0;
+    for (; i + 2 <= e.n.ns; i += 2) {
+        const bool h0 = hit_sphere(p[i], x, y, z, r), h1 = hit_sphere(p[i + 1], x, y, z, r);
+        if (h0 | h1) return 2 * (w + (h0 ? 1 : 2) * kFlopSphere) + 1;
+        w += 2 * kFlopSphere;
+    }
+    if (i < e.n.ns) {
         w += kFlopSphere;
         if (hit_sphere(p[i], x, y, z, r)) return 2 * w + 1;
     }
     p += e.n.ns;
-    for (int i = 0; i < e.n.nc; i++) {
+    for (i = 0; i + 2 <= e.n.nc; i += 2) {
+        const float4 *c = p + 2 * i;
+        const bool h0 = hit_capsule(c[0], c[1], x, y, z, r), h1 = hit_capsule(c[2], c[3], x, y, z, r);
+        if (h0 | h1) return 2 * (w + (h0 ? 1 : 2) * kFlopCapsule) + 1;
+        w += 2 * kFlopCapsule;
+    }
+    if (i < e.n.nc) {
         w += kFlopCapsule;
         if (hit_capsule(p[2 * i], p[2 * i + 1], x, y, z, r)) return 2 * w + 1;
     }
     p += 2 * e.n.nc;
-    for (int i = 0; i < e.n.nzc; i++) {
+    for (i = 0; i < e.n.nzc; i++) {
         w += kFlopZCapsule;
         if (hit_z_capsule(p[2 * i], p[2 * i + 1], x, y, z, r)) return 2 * w + 1;
     }
     p += 2 * e.n.nzc;
     const float rsq = r * r;
-    for (int i = 0; i < e.n.ncb; i++) {
+    for (i = 0; i + 2 <= e.n.ncb; i += 2) {
+        const float4 *c = p + 4 * i;
+        const bool h0 = hit_cuboid(c[0], c[1], c[2], c[3], x, y, z, rsq),
+                   h1 = hit_cuboid(c[4], c[5], c[6], c[7], x, y, z, rsq);
+        if (h0 | h1) return 2 * (w + (h0 ? 1 : 2) * kFlopCuboid) + 1;
+        w += 2 * kFlopCuboid;
+    }
+    if (i < e.n.ncb) {
         w += kFlopCuboid;
         if (hit_cuboid(p[4 * i], p[4 * i + 1], p[4 * i + 2], p[4 * i + 3], x, y, z, rsq)) return 2 * w + 1;
     }
     p += 4 * e.n.ncb;
-    for (int i = 0; i < e.n.nzb; i++) {
+    for (i = 0; i < e.n.nzb; i++) {
         w += kFlopZCuboid;
         if (hit_z_cuboid(p[4 * i], p[4 * i + 1], p[4 * i + 2], x, y, z, rsq)) return 2 * w + 1;
     }
@@ -162,15 +184,19 @@ static __device__ __noinline__ int env_leaves(const EnvView e, const Frame T, co
 // inflation of a pair (twice the per-sphere pad).  Returns 2 * FLOPs + hit.
 static __device__ __noinline__ int self_pairs(const Frame Tab, const LeafPair *__restrict__ pairs, int n, float pad2)
 {
-    for (int i = 0; i < n; i++) {
-        const float4 a = pairs[i].a;
-        const float4 b = pairs[i].b;
+    auto hit = [&](const LeafPair &pr) {
         float x, y, z;
-        xform(Tab, b, x, y, z);
-        const float dx = a.x - x, dy = a.y - y, dz = a.z - z;
-        const float rs = a.w + b.w + pad2;
-        if (dx * dx + dy * dy + dz * dz - rs * rs < 0.0f) return 2 * kFlopPair * (i + 1) + 1;
+        xform(Tab, pr.b, x, y, z);
+        const float dx = pr.a.x - x, dy = pr.a.y - y, dz = pr.a.z - z;
+        const float rs = pr.a.w + pr.b.w + pad2;
+        return dx * dx + dy * dy + dz * dz - rs * rs < 0.0f;
+    };
+    int i = 0;
+    for (; i + 2 <= n; i += 2) {   // two at a time, counted up to the first hit
+        const bool h0 = hit(pairs[i]), h1 = hit(pairs[i + 1]);
+        if (h0 | h1) return 2 * kFlopPair * (i + (h0 ? 1 : 2)) + 1;
     }
+    if (i < n && hit(pairs[i])) return 2 * kFlopPair * (i + 1) + 1;
     return 2 * kFlopPair * n;
 }
 
