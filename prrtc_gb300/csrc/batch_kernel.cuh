@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                     const unsigned b = (unsigned)P.halton_bases[vl % P.bases_lanes * 16 + d];
                     const unsigned hs = hash32((unsigned)q * 0x9E3779B1u + (unsigned)attempt * 0xC2B2AE35u +
                                                (unsigned)d * 0x85EBCA77u + 0x165667B1u);
-                    h = scrambled_radical_inverse((unsigned)iter, b, 1u + hs % (b - 1u));
+                    h = scrambled_radical_inverse((unsigned)iter, b, 1u + hs - div_by(hs, kDivTable.magic[b - 1u]) * (b - 1u));
                     h += (float)(hs >> 8) * (1.0f / 16777216.0f);
                     h -= floorf(h);
                 }

@@ -212,15 +212,46 @@ __device__ __forceinline__ void warp_nn(const float *__restrict__ nodes, int cap
     out_i = bi == 0x7fffffff ? 0 : bi;
 }
 
+// Exact unsigned division by a small divisor b (2..64) without a divide
+// instruction: q = floor(i * M / 2^k) with k = 32 + ceil(log2 b) and
+// M = floor(2^k / b) + 1, which equals floor(i / b) for every 32-bit i
+// because 2^k < M * b <= 2^k + b <= 2^k + 2^(k-32) (Granlund and
+// Montgomery, "Division by invariant integers using multiplication", 1994).
+// magic[b] holds M * 2^(64-k), so q is the high word of one 64-bit product.
+// The sampler's digit loops divide by the Halton bases this way; a rejected
+// sample of a dynamic-domain query is almost nothing but those loops.
+struct DivTable {
+    unsigned long long magic[65];
+    float inv[65];   // 1 / b, correctly rounded
+    constexpr DivTable() : magic(), inv()
+    {
+        for (unsigned b = 2; b <= 64; b++) {
+            unsigned ell = 0;
+            while ((1u << ell) < b) ell++;
+            const unsigned k = 32 + ell;
+            magic[b] = ((1ull << k) / b + 1) << (64 - k);
+            inv[b] = 1.0f / (float)b;
+        }
+    }
+};
+__constant__ const DivTable kDivTable = DivTable();
+
+__device__ __forceinline__ unsigned div_by(unsigned i, unsigned long long magic)
+{
+    return (unsigned)__umul64hi((unsigned long long)i, magic);
+}
+
 // Radical inverse of index i in integer base b, float32 (the closed form of
 // the reference's incremental Halton recurrence).
 __device__ __forceinline__ float radical_inverse(unsigned i, unsigned b)
 {
-    const float inv = 1.0f / (float)b;
+    const unsigned long long s = kDivTable.magic[b];
+    const float inv = kDivTable.inv[b];
     float f = inv, r = 0.0f;
     while (i > 0) {
-        r = fmaf(f, (float)(i % b), r);
-        i /= b;
+        const unsigned q = div_by(i, s);
+        r = fmaf(f, (float)(i - q * b), r);
+        i = q;
         f *= inv;
     }
     return r;
@@ -232,11 +263,14 @@ __device__ __forceinline__ float radical_inverse(unsigned i, unsigned b)
 // low-discrepancy structure.
 __device__ __forceinline__ float scrambled_radical_inverse(unsigned i, unsigned b, unsigned a)
 {
-    const float inv = 1.0f / (float)b;
+    const unsigned long long s = kDivTable.magic[b];
+    const float inv = kDivTable.inv[b];
     float f = inv, r = 0.0f;
     while (i > 0) {
-        r = fmaf(f, (float)((a * (i % b)) % b), r);
-        i /= b;
+        const unsigned q = div_by(i, s);
+        const unsigned ad = a * (i - q * b);
+        r = fmaf(f, (float)(ad - div_by(ad, s) * b), r);
+        i = q;
         f *= inv;
     }
     return r;
