@@ -4,7 +4,7 @@ prrtc_smooth_paths) against the oracle.
 Inputs are planned paths: Panda tabletop and shelf and Baxter tabletop queries
 solved by the batched planner, resampled to 64 float32 waypoints.  The
 library's adjoint must match the oracle's float64 adjoint to 1e-4 (relative,
-per waypoint, floored at 1e-6 for waypoints whose gradient vanishes) and the
+per waypoint, plus 1e-9 absolute for waypoints whose gradient vanishes) and the
 central finite differences of the library's own cost at h = 1e-3 rad within
 the truncation bound the hinge allows.  Every smoothed path the library
 accepts must pass the oracle's checker at 128 points per edge, and every path
@@ -61,8 +61,13 @@ def test_adjoint_matches_fp64(ctx, oracle, planned, robot):
         c64[i], g64[i] = oracle.cost_grad(robot, e, P[i].astype(np.float64), MARGIN)
     assert (c64 > 0).any()
     np.testing.assert_allclose(cost, c64, rtol=1e-4, atol=1e-9)
-    rel = floored_rel(grad, g64)
-    assert rel.max() <= 1e-4, (rel.max(), np.median(rel))
+    # per waypoint: relative 1e-4, plus 1e-9 absolute (the float32 resolution of
+    # gradient entries of order 1e-2; a waypoint whose true gradient is ~1e-6
+    # is otherwise judged on rounding alone)
+    err = np.linalg.norm((grad - g64).reshape(-1, grad.shape[-1]), axis=1)
+    ref = np.linalg.norm(g64.reshape(-1, grad.shape[-1]), axis=1)
+    worst = np.max(err - 1e-4 * ref)
+    assert worst <= 1e-9, (worst, np.median(floored_rel(grad, g64)))
     assert np.linalg.norm(grad - g64) / np.linalg.norm(g64) <= 1e-4
 
 
@@ -179,7 +184,8 @@ def test_autograd_shim_descent(ctx, oracle, planned):
     q = torch.from_numpy(P).cuda().requires_grad_(True)
     cost_fn(q).sum().backward()
     g64 = np.stack([oracle.cost_grad("panda", e, P[i].astype(np.float64), MARGIN)[1] for i, e in enumerate(envs)])
-    assert floored_rel(q.grad.cpu().numpy(), g64).max() <= 1e-4
+    g = q.grad.cpu().numpy()
+    assert np.max(np.linalg.norm(g - g64, axis=-1) - 1e-4 * np.linalg.norm(g64, axis=-1)) <= 1e-9
     # the library's smoothing iteration (without the joint-limit clamp),
     # driven from torch: d/dx of 1/2 sum |x_{w+1} - x_w|^2 is the path Laplacian
     x = torch.from_numpy(P).cuda()
