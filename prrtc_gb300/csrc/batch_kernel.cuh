@@ -26,7 +26,13 @@
 
 namespace prrtc {
 
+// Obstacle records a warp keeps in shared memory for the query it works on
+// (4 KB: Panda and Fetch scenes and most Baxter ones); larger scenes are
+// read from global memory through L1.
+constexpr int kWarpEnvRecords = 256;
+
 struct WarpScratch {
+    float4 env[kWarpEnvRecords];
     float from[16], step[16], cfg[16], nn[16], vec[16], next[16];
     float chunk[16][33];   // 32 tree nodes staged for the round's nearest-neighbour pass (+1: bank skew)
     int bad;
@@ -360,6 +366,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
     if (lane == 0) atomicCAS(&C->t0, 0ull, global_ns());
     int slot = -1;
     unsigned idle = 0;
+    const float4 *staged = nullptr;   // the global records now in W.env
     unsigned long long nn_visits = 0;   // flushed once per warp (a shared counter would serialise)
     auto flush = [&]() {
         if (lane == 0 && nn_visits) atomicAdd(&C->nn_nodes, nn_visits);
@@ -489,7 +496,17 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
         const int q = vload(&S->query);
         const int attempt = vload(&S->attempt);
         const BatchQueryDesc Qd = P.queries[q];
-        CheckCtx ctx{{Qd.env, Qd.env_n}, P.pad, &W.bad};
+        const float4 *envp = Qd.env;
+        if (Qd.env_n.records() <= kWarpEnvRecords) {
+            if (staged != Qd.env) {   // the records are read-only for the whole launch
+                __syncwarp();
+                for (int i = lane; i < Qd.env_n.records(); i += 32) W.env[i] = __ldg(Qd.env + i);
+                __syncwarp();
+                staged = Qd.env;
+            }
+            envp = W.env;
+        }
+        CheckCtx ctx{{envp, Qd.env_n}, P.pad, &W.bad};
         float *nodes_s = P.nodes + (size_t)slot * 2 * D * P.cap;
         int *par_s = P.parents + (size_t)slot * 2 * P.cap;
         float *rad_s = P.radii + (size_t)slot * 2 * P.cap;
