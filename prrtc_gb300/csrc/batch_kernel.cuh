@@ -556,22 +556,39 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                 t = ratio < P.tree_ratio ? 1 - prev : prev;
             }
             float qv[D];
+            // dimensions in ceil(D / 7) equal groups, each group's digit chains interleaved
+            constexpr int NG = (D + 6) / 7, G = (D + NG - 1) / NG;
 #pragma unroll
-            for (int d = 0; d < D; d++) {
-                float h;
-                if (P.sampler == 0) {
-                    const int row = (vl + attempt * P.lanes) % P.bases_lanes;
-                    h = radical_inverse((unsigned)iter, (unsigned)P.halton_bases[row * 16 + d]);
-                } else {
+            for (int d0 = 0; d0 < D; d0 += G) {
+                unsigned bs[G], as[G], hsh[G];
+                float hv[G];
+                const int row = P.sampler == 0 ? (vl + attempt * P.lanes) % P.bases_lanes : vl % P.bases_lanes;
+#pragma unroll
+                for (int j = 0; j < G; j++) {
+                    const int d = d0 + j < D ? d0 + j : D - 1;   // a short last group repeats a dimension
+                    bs[j] = (unsigned)P.halton_bases[row * 16 + d];
                     // scrambled Halton: digit multiplier and rotation per (query, attempt, dimension)
-                    const unsigned b = (unsigned)P.halton_bases[vl % P.bases_lanes * 16 + d];
-                    const unsigned hs = hash32((unsigned)q * 0x9E3779B1u + (unsigned)attempt * 0xC2B2AE35u +
-                                               (unsigned)d * 0x85EBCA77u + 0x165667B1u);
-                    h = scrambled_radical_inverse((unsigned)iter, b, 1u + hs - div_by(hs, kDivTable.magic[b - 1u]) * (b - 1u));
-                    h += (float)(hs >> 8) * (1.0f / 16777216.0f);
-                    h -= floorf(h);
+                    hsh[j] = P.sampler == 0 ? 0u
+                                            : hash32((unsigned)q * 0x9E3779B1u + (unsigned)attempt * 0xC2B2AE35u +
+                                                     (unsigned)d * 0x85EBCA77u + 0x165667B1u);
+                    as[j] = 1u + hsh[j] - div_by(hsh[j], kDivTable.magic[bs[j] - 1u]) * (bs[j] - 1u);
                 }
-                qv[d] = fmaf(h, P.scale[d], P.offset[d]);
+                if (P.sampler == 0)
+                    radical_inverses<G, false>((unsigned)iter, bs, as, hv);
+                else
+                    radical_inverses<G, true>((unsigned)iter, bs, as, hv);
+#pragma unroll
+                for (int j = 0; j < G; j++) {
+                    const int d = d0 + j;
+                    if (d < D) {
+                        float h = hv[j];
+                        if (P.sampler != 0) {
+                            h += (float)(hsh[j] >> 8) * (1.0f / 16777216.0f);
+                            h -= floorf(h);
+                        }
+                        qv[d] = fmaf(h, P.scale[d], P.offset[d]);
+                    }
+                }
             }
             // -- nearest node of every lane's sample: one pass per tree, nodes
             // staged 32 at a time in shared memory and read by all lanes

@@ -276,6 +276,45 @@ __device__ __forceinline__ float scrambled_radical_inverse(unsigned i, unsigned 
     return r;
 }
 
+// Radical inverses of one index in N bases at once (h[d] in base b[d], each
+// digit multiplied by a[d] mod b[d] when SCRAMBLE).  The digit chains of the N
+// dimensions advance together, one digit of every dimension per trip, for as
+// many trips as the smallest base needs: N independent dependency chains
+// instead of N loops in a row, and the same trip count on every lane.  A
+// dimension whose index is exhausted adds fmaf(f, 0, h) = h, so every h[d] is
+// bit-identical to radical_inverse / scrambled_radical_inverse.
+template <int N, bool SCRAMBLE>
+__device__ __forceinline__ void radical_inverses(unsigned iter, const unsigned (&b)[N], const unsigned (&a)[N],
+                                                 float (&h)[N])
+{
+    unsigned idx[N];
+    float f[N];
+    unsigned bmin = b[0];
+#pragma unroll
+    for (int d = 0; d < N; d++) {
+        idx[d] = iter;
+        f[d] = kDivTable.inv[b[d]];
+        h[d] = 0.0f;
+        bmin = min(bmin, b[d]);
+    }
+    const unsigned long long mmin = kDivTable.magic[bmin];
+    for (unsigned rem = iter; rem > 0; rem = div_by(rem, mmin)) {
+#pragma unroll
+        for (int d = 0; d < N; d++) {
+            const unsigned long long mg = kDivTable.magic[b[d]];
+            const unsigned q = div_by(idx[d], mg);
+            unsigned dig = idx[d] - q * b[d];
+            if (SCRAMBLE) {
+                const unsigned t = a[d] * dig;
+                dig = t - div_by(t, mg) * b[d];
+            }
+            h[d] = fmaf(f[d], (float)dig, h[d]);
+            idx[d] = q;
+            f[d] *= kDivTable.inv[b[d]];
+        }
+    }
+}
+
 __device__ __forceinline__ unsigned hash32(unsigned x)
 {
     x ^= x >> 16;
