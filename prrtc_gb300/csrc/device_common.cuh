@@ -200,6 +200,48 @@ static __device__ __noinline__ int self_pairs(const Frame Tab, const LeafPair *_
     return 2 * kFlopPair * n;
 }
 
+// ---- table-driven checker (robots with many groups) -----------------------
+// A generated checker for a robot with hundreds of groups (Baxter: 388) as
+// straight-line code does not fit the instruction cache; its table form
+// computes every frame first and then walks the same schedule through these
+// tables, making the same ctx calls in the same order (same verdicts, same
+// counts).  Frames are indexed by joint config index + 1; F[0] is the world.
+
+struct GenSched {
+    int kind;    // 0 environment group, 1 self group
+    int index;
+};
+struct GenEnvGroup {
+    float4 gate;          // gating sphere in its frame (x, y, z, r)
+    int gate_frame;       // -1 world; ignored when !has_gate
+    int has_gate;
+    int first_block, nblocks;
+};
+struct GenLeafBlock {
+    int frame, first, n, pad_;
+};
+struct GenSelfGroup {
+    float4 a, b;          // gating pair, each in its frame
+    int fa, fb, first_block, nblocks;
+};
+struct GenPairBlock {
+    int fa, fb, first, n;
+};
+
+// Tab = inv(A) * B for rigid transforms A and B.
+__device__ __forceinline__ Frame relative_frame(const Frame &A, const Frame &B)
+{
+    Frame R;
+    const float d0 = B.m[3] - A.m[3], d1 = B.m[7] - A.m[7], d2 = B.m[11] - A.m[11];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) R.m[4 * i + k] = A.m[i] * B.m[k] + A.m[4 + i] * B.m[4 + k] + A.m[8 + i] * B.m[8 + k];
+        R.m[4 * i + 3] = A.m[i] * d0 + A.m[4 + i] * d1 + A.m[8 + i] * d2;
+    }
+    return R;
+}
+
 // What the generated checkers call.  pad = 0 and stop_flag = nullptr give the
 // reference checker's verdicts; planners may inflate every sphere by pad
 // (a certified margin) and share a flag through which any lane's collision
@@ -235,5 +277,44 @@ struct CheckCtx {
     }
     __device__ __forceinline__ bool stop() const { return stop_flag != nullptr && *stop_flag != 0; }
 };
+
+// The schedule of a table-form checker (see GenSched); returns true when free.
+template <class Ctx>
+__device__ __noinline__ bool run_schedule(const Frame *F, const GenSched *__restrict__ sched, int nsched,
+                                          const GenEnvGroup *__restrict__ eg, const GenLeafBlock *__restrict__ lb,
+                                          const float4 *__restrict__ leaves, const GenSelfGroup *__restrict__ sg,
+                                          const GenPairBlock *__restrict__ pb, const LeafPair *__restrict__ pairs,
+                                          Ctx &ctx)
+{
+    for (int s = 0; s < nsched; s++) {
+        const GenSched e = sched[s];
+        if (e.kind == 0) {
+            const GenEnvGroup g = eg[e.index];
+            bool go = true;
+            if (g.has_gate) {
+                float x, y, z;
+                xform(F[g.gate_frame + 1], g.gate, x, y, z);
+                go = ctx.env_hit(x, y, z, g.gate.w);
+            }
+            if (go)
+                for (int k = g.first_block; k < g.first_block + g.nblocks; k++) {
+                    const GenLeafBlock b = lb[k];
+                    if (ctx.env_leaves(F[b.frame + 1], leaves + b.first, b.n)) return false;
+                }
+        } else {
+            const GenSelfGroup g = sg[e.index];
+            float ax, ay, az, bx, by, bz;
+            xform(F[g.fa + 1], g.a, ax, ay, az);
+            xform(F[g.fb + 1], g.b, bx, by, bz);
+            if (ctx.pair_hit(ax - bx, ay - by, az - bz, g.a.w + g.b.w))
+                for (int k = g.first_block; k < g.first_block + g.nblocks; k++) {
+                    const GenPairBlock b = pb[k];
+                    if (ctx.self_pairs(relative_frame(F[b.fa + 1], F[b.fb + 1]), pairs + b.first, b.n)) return false;
+                }
+        }
+        if (ctx.stop()) return true;
+    }
+    return true;
+}
 
 }  // namespace prrtc

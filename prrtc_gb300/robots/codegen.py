@@ -32,6 +32,11 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE.parent / "csrc" / "robots"
 ROBOTS = ("sphere", "panda", "fetch", "baxter")
 INLINE_LEAVES = 6   # leaf blocks up to this size are emitted as straight-line tests
+# Robots whose checker is emitted in table form: every frame computed first,
+# then one loop over the group schedule (run_schedule in device_common.cuh).
+# Baxter's 388 groups as straight-line code overflow the instruction cache
+# (its planner kernel stalled on instruction fetch 33 times per issue).
+TABLE_ROBOTS = ("baxter",)
 
 
 def load_model(robot: str) -> dict:
@@ -309,7 +314,18 @@ def emit_cuda_checker(m: dict) -> str:
                 calls.append(f"ctx.env_leaves({_frame_arg(T)}, k{R}Leaf + {first}, {n})")
         return calls
 
-    for kind, gi in m["schedule"]:
+    table = name in TABLE_ROBOTS
+    if table:
+        # every frame, in chain order, into F[q + 1]; then the schedule loop
+        nj = len(m["joints"])
+        frames = [fk.frame(jt["q"]) for jt in m["joints"]]
+        code.lines.append(f"Frame F[{nj + 1}];")
+        code.lines.append("F[0] = Frame{{1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f}};")
+        for jt, T in zip(m["joints"], frames):
+            code.lines.append(f"F[{jt['q'] + 1}] = {_frame_arg(T)};")
+        code.lines.append(f"return run_schedule(F, k{R}Sched, {len(m['schedule'])}, k{R}EnvGroup, k{R}LeafBlock, k{R}Leaf, "
+                          f"k{R}SelfGroup, k{R}PairBlock, k{R}Pair, ctx);")
+    for kind, gi in ([] if table else m["schedule"]):
         if kind == "env":
             g = m["env_groups"][gi]
             code.lines.append(f"// environment group {gi}: {g['label']}")
@@ -342,7 +358,8 @@ def emit_cuda_checker(m: dict) -> str:
                 code.lines.append(f"    if (ctx.self_pairs({_frame_arg(M)}, k{R}Pair + {first}, {n})) return false;")
             code.lines.append("}")
         code.lines.append("if (ctx.stop()) return true;")
-    code.lines.append("return true;")
+    if not table:
+        code.lines.append("return true;")
 
     # fk_spheres: every sphere's world centre (not on the validation hot path)
     code2 = _Code()
@@ -379,6 +396,47 @@ def emit_cuda_checker(m: dict) -> str:
     for ca, ra, cb, rb in pair_rows or [([0, 0, 0], 0.0, [0, 0, 0], 0.0)]:
         w("    {{%s, %s, %s, %s}, {%s, %s, %s, %s}}," % (*[_lit(v) for v in ca], _lit(ra), *[_lit(v) for v in cb], _lit(rb)))
     w("};")
+    if table:
+        w("// the schedule in table form (run_schedule)")
+        w(f"__device__ const GenSched k{R}Sched[{len(m['schedule'])}] = {{")
+        for kind, gi in m["schedule"]:
+            w(f"    {{{0 if kind == 'env' else 1}, {gi}}},")
+        w("};")
+        lblocks, eg_rows = [], []
+        for gi, g in enumerate(m["env_groups"]):
+            first = len(lblocks)
+            for f, fl, n in env_blocks[gi]:
+                lblocks.append((f, fl, n))
+            if g["gate"] >= 0:
+                s = sp[g["gate"]]
+                eg_rows.append(((s["c"][0], s["c"][1], s["c"][2], s["r"]), s["frame"], 1, first, len(lblocks) - first))
+            else:
+                eg_rows.append(((0.0, 0.0, 0.0, 0.0), -1, 0, first, len(lblocks) - first))
+        w(f"__device__ const GenEnvGroup k{R}EnvGroup[{max(1, len(eg_rows))}] = {{")
+        for gate, f, has, first, nb in eg_rows or [((0.0, 0.0, 0.0, 0.0), -1, 0, 0, 0)]:
+            w("    {{%s}, %d, %d, %d, %d}," % (", ".join(_lit(v) for v in gate), f, has, first, nb))
+        w("};")
+        w(f"__device__ const GenLeafBlock k{R}LeafBlock[{max(1, len(lblocks))}] = {{")
+        for f, fl, n in lblocks or [(-1, 0, 0)]:
+            w(f"    {{{f}, {fl}, {n}, 0}},")
+        w("};")
+        pblocks, sg_rows = [], []
+        for gi, g in enumerate(m["self_groups"]):
+            first = len(pblocks)
+            for fa, fb, pf, n in self_blocks[gi]:
+                pblocks.append((fa, fb, pf, n))
+            a, b = g["gate"]
+            sa, sb = sp[a], sp[b]
+            sg_rows.append(((*sa["c"], sa["r"]), (*sb["c"], sb["r"]), sa["frame"], sb["frame"], first, len(pblocks) - first))
+        w(f"__device__ const GenSelfGroup k{R}SelfGroup[{max(1, len(sg_rows))}] = {{")
+        for ga, gb, fa, fb, first, nb in sg_rows or [((0.0,) * 4, (0.0,) * 4, -1, -1, 0, 0)]:
+            w("    {{%s}, {%s}, %d, %d, %d, %d}," % (", ".join(_lit(v) for v in ga), ", ".join(_lit(v) for v in gb),
+                                                   fa, fb, first, nb))
+        w("};")
+        w(f"__device__ const GenPairBlock k{R}PairBlock[{max(1, len(pblocks))}] = {{")
+        for fa, fb, pf, n in pblocks or [(-1, -1, 0, 0)]:
+            w(f"    {{{fa}, {fb}, {pf}, {n}}},")
+        w("};")
     w("")
     w("// Returns true when configuration q is collision-free.")
     w("template <class Ctx>")
