@@ -36,7 +36,7 @@ INLINE_LEAVES = 6   # leaf blocks up to this size are emitted as straight-line t
 # then one loop over the group schedule (run_schedule in device_common.cuh).
 # Baxter's 388 groups as straight-line code overflow the instruction cache
 # (its planner kernel stalled on instruction fetch 33 times per issue).
-TABLE_ROBOTS = ("fetch", "baxter")
+TABLE_ROBOTS = ("panda", "fetch", "baxter")
 
 
 def load_model(robot: str) -> dict:
