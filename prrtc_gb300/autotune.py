@@ -19,7 +19,7 @@ Sweeps, on a calibration batch of seeded queries, the knobs of
 and keeps the setting with the highest solved queries per second.  Results
 are cached in ``tuning.json`` next to this file, keyed by robot and workload:
 
-    python -m prrtc_gb300.autotune panda_shelf [queries]   # on a GPU; rewrites the entry
+    python -m prrtc_gb300.autotune panda_shelf [queries] [budget_s]   # on a GPU; rewrites the entry
 """
 from __future__ import annotations
 
@@ -31,8 +31,8 @@ from pathlib import Path
 TUNING = Path(__file__).resolve().parent / "tuning.json"
 DEFAULT = {"lanes": 1, "warps_per_block": 2, "edge_order": 0, "sampler": 0, "max_workers_per_attempt": 0,
            "max_attempts": 4}
-SPACE = {"lanes": (1, 2), "warps_per_block": (2,), "edge_order": (0,), "sampler": (0, 1),
-         "max_workers_per_attempt": (64, 256, 0), "max_attempts": (4,)}
+SPACE = {"lanes": (1, 2), "warps_per_block": (2, 4), "edge_order": (0, 1), "sampler": (0, 1),
+         "max_workers_per_attempt": (64, 0), "max_attempts": (4,)}
 KNOBS = tuple(SPACE)
 
 
@@ -48,16 +48,17 @@ def load(robot: str, workload: str | None = None) -> dict:
     return dict(DEFAULT)
 
 
-def tune(ctx, robot, queries, plan, margin=1e-5, reps=3, space=None) -> dict:
+def tune(ctx, robot, queries, plan, margin=1e-5, reps=3, space=None, budget_ns=int(60e9)) -> dict:
     """Run every setting `reps` times and keep the one with the best median
-    batch time among those that solve the most queries."""
+    batch time among those that solve the most queries.  With a time budget
+    shorter than the batch needs, the most queries solved within it decides."""
     import statistics
     from .api import BatchSettings
     space = space or SPACE
     rows = []
     for values in itertools.product(*(space[k] for k in KNOBS)):
         knobs = dict(zip(KNOBS, values))
-        bs = BatchSettings(plan, use_graph=1, margin=margin, **knobs)
+        bs = BatchSettings(plan, use_graph=1, margin=margin, time_budget_ns=budget_ns, **knobs)
         b = ctx.batch(robot, queries, bs)
         b.run()
         times, solved = [], []
@@ -82,11 +83,13 @@ def main(argv):
     from bench import WORKLOAD_SETTINGS   # the benchmark's settings per workload
     name = argv[1] if len(argv) > 1 else "panda_shelf"
     n = int(argv[2]) if len(argv) > 2 else 1024
+    budget_s = float(argv[3]) if len(argv) > 3 else 60.0
     robot = workloads.WORKLOADS[name][0]
     qs = workloads.make(name, n, seed0=100_000)    # calibration queries, disjoint from the benchmark's
     ctx = Context(0)
     envs = [ctx.upload_env(q.env) for q in qs]
-    out = tune(ctx, robot, [(e, q.start, q.goal) for e, q in zip(envs, qs)], Settings(**WORKLOAD_SETTINGS[name]))
+    out = tune(ctx, robot, [(e, q.start, q.goal) for e, q in zip(envs, qs)], Settings(**WORKLOAD_SETTINGS[name]),
+               budget_ns=int(budget_s * 1e9))
     table = json.loads(TUNING.read_text()) if TUNING.exists() else {}
     table[f"{robot}/{name}"] = out
     TUNING.write_text(json.dumps(table, indent=1) + "\n")
