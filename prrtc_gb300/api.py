@@ -35,12 +35,13 @@ class PrrtcError(RuntimeError):
 
 
 class EnvDesc(C.Structure):
-    _fields_ = [("spheres", C.POINTER(C.c_float)), ("num_spheres", C.c_uint32),
-                ("capsules", C.POINTER(C.c_float)), ("num_capsules", C.c_uint32),
-                ("z_aligned_capsules", C.POINTER(C.c_float)), ("num_z_aligned_capsules", C.c_uint32),
-                ("cylinders", C.POINTER(C.c_float)), ("num_cylinders", C.c_uint32),
-                ("cuboids", C.POINTER(C.c_float)), ("num_cuboids", C.c_uint32),
-                ("z_aligned_cuboids", C.POINTER(C.c_float)), ("num_z_aligned_cuboids", C.c_uint32)]
+    # const float * fields held as addresses (same size and layout as the C struct)
+    _fields_ = [("spheres", C.c_void_p), ("num_spheres", C.c_uint32),
+                ("capsules", C.c_void_p), ("num_capsules", C.c_uint32),
+                ("z_aligned_capsules", C.c_void_p), ("num_z_aligned_capsules", C.c_uint32),
+                ("cylinders", C.c_void_p), ("num_cylinders", C.c_uint32),
+                ("cuboids", C.c_void_p), ("num_cuboids", C.c_uint32),
+                ("z_aligned_cuboids", C.c_void_p), ("num_z_aligned_cuboids", C.c_uint32)]
 
 
 class Settings(C.Structure):
@@ -380,18 +381,28 @@ class Context:
         b.handle = None
         keep = []
         qs = (_Query * b.n)()
-        for i, q in enumerate(queries):
-            env, start, goals = q if isinstance(q, tuple) else (q.env, q.start, q.goal)
-            start = np.ascontiguousarray(np.asarray(start, np.float32).reshape(b.D))
-            goals = np.ascontiguousarray(np.asarray(goals, np.float32).reshape(-1, b.D))
-            keep += [start, goals]
+        trip = [q if isinstance(q, tuple) else (q.env, q.start, q.goal) for q in queries]
+        # every start and goal in two contiguous arrays; each query points into them
+        starts = np.ascontiguousarray(np.stack([np.asarray(s, np.float32).reshape(b.D) for _, s, _ in trip]))
+        goal_list = [np.asarray(g, np.float32).reshape(-1, b.D) for _, _, g in trip]
+        goals = np.ascontiguousarray(np.concatenate(goal_list))
+        keep += [starts, goals]
+        s0, g0, row = starts.ctypes.data, goals.ctypes.data, 4 * b.D
+        descs = (EnvDesc * b.n)()
+        d0, dsz = C.addressof(descs), C.sizeof(EnvDesc)
+        keep.append(descs)
+        goff = 0
+        for i, (env, _, _) in enumerate(trip):
             if isinstance(env, EnvHandle):
                 qs[i].env = env.handle
             else:
                 d, k = _env_desc(env)
-                keep += [d, k]
-                qs[i].env_desc = C.cast(C.pointer(d), C.c_void_p)
-            qs[i].start, qs[i].goals, qs[i].num_goals = start.ctypes.data, goals.ctypes.data, len(goals)
+                descs[i] = d
+                keep.append(k)
+                qs[i].env_desc = d0 + i * dsz
+            ng = len(goal_list[i])
+            qs[i].start, qs[i].goals, qs[i].num_goals = s0 + i * row, g0 + goff * row, ng
+            goff += ng
         res = (_Result * b.n)()
         paths = np.empty((b.n, path_capacity, b.D), np.float32)
         for i in range(b.n):
@@ -488,15 +499,19 @@ class Batch:
             pass
 
 
+_ENV_KINDS = ("spheres", "capsules", "z_aligned_capsules", "cylinders", "cuboids", "z_aligned_cuboids")
+
+
 def _env_desc(env: Environment):
-    d = EnvDesc()
-    keep = []
-    for k in ("spheres", "capsules", "z_aligned_capsules", "cylinders", "cuboids", "z_aligned_cuboids"):
-        a = np.ascontiguousarray(getattr(env, k), np.float32)
+    keep, args = [], []
+    for k in _ENV_KINDS:
+        a = getattr(env, k)
+        if a.dtype != np.float32 or not a.flags.c_contiguous:
+            a = np.ascontiguousarray(a, np.float32)
         keep.append(a)
-        setattr(d, k, a.ctypes.data_as(C.POINTER(C.c_float)) if len(a) else None)
-        setattr(d, "num_" + k, len(a))
-    return d, keep
+        n = len(a)
+        args += (a.ctypes.data if n else None, n)
+    return EnvDesc(*args), keep
 
 
 def _empty_like_device(t, shape, dtype: str):
