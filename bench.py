@@ -170,6 +170,26 @@ def config_of(args):
                   "(stream input > L2)", "parallelism": "queries sharded over ranks"}
 
 
+def shard_seed0(rank: int, n: int, steps: int) -> int:
+    """First query seed of a rank: ranks plan disjoint query sets (weak scaling)."""
+    return rank * n * steps
+
+
+def reduce_over_ranks(t_dev: float, solved: int, world: int, device: str = "cpu"):
+    """Whole-job figures over ranks: the slowest rank's device time and the
+    total of solved queries (queries shard with no exchange on the data path;
+    these two numbers are the only collective)."""
+    if world <= 1:
+        return t_dev, solved
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([t_dev], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    c = torch.tensor([float(solved)], dtype=torch.float64, device=device)
+    dist.all_reduce(c)
+    return float(t.item()), int(c.item())
+
+
 def h2d_bytes(qs):
     b = 0
     for q in qs:
@@ -189,7 +209,7 @@ def ours(args, rank, world):
     robot = workloads.WORKLOADS[args.workload][0]
     n = args.queries
     # K steps of n queries each, distinct seeds, streamed through one launch
-    qs = workloads.make(args.workload, n * args.steps, seed0=rank * n * args.steps)
+    qs = workloads.make(args.workload, n * args.steps, seed0=shard_seed0(rank, n, args.steps))
     first = qs[:n]
     plan = settings_for(args.workload)
     ctx = Context(dev)
@@ -223,13 +243,7 @@ def ours(args, rank, world):
     results = stream.results()
     solved = sum(r.solved for r in results)
     t_dev = st["kernel_ns"] * 1e-9
-    if world > 1:
-        t = torch.tensor([t_dev], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(t.item())
-        c = torch.tensor([float(solved)], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(c)
-        solved = int(c.item())
+    t_dev, solved = reduce_over_ranks(t_dev, solved, world, f"cuda:{dev}")
     value = solved / t_dev
     lat = [r.kernel_ns / 1e6 for r in results if r.solved]
 
