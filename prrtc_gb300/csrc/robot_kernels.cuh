@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(256) k_validate_configs(const float4 *__restri
         float cfg[Gen::kDof];
         load_cfg<Gen::kDof>(q, i, cfg);
         ctx.work = 0;
-        out[i] = Gen::fkcc(cfg, ctx) ? 1 : 0;
+        out[i] = Gen::fkcc_validate(cfg, ctx) ? 1 : 0;
         flops += ctx.work + Gen::kFkFlops;
         cfgs++;
     }
@@ -431,6 +431,11 @@ struct RobotKernels {
         static __device__ __forceinline__ bool fkcc(const float *q, Ctx &ctx)                       \
         {                                                                                           \
             return NS::fkcc(q, ctx);                                                                \
+        }                                                                                           \
+        template <class Ctx>                                                                        \
+        static __device__ __forceinline__ bool fkcc_validate(const float *q, Ctx &ctx)              \
+        {                                                                                           \
+            return NS::fkcc_validate(q, ctx);                                                       \
         }                                                                                           \
         static __device__ __forceinline__ void fk_spheres(const float *q, float4 *out)              \
         {                                                                                           \

@@ -45,6 +45,13 @@ __device__ __forceinline__ bool fkcc(const float *__restrict__ q, Ctx &ctx)
     return true;
 }
 
+// The same verdicts for the stand-alone checker of single configurations.
+template <class Ctx>
+__device__ __forceinline__ bool fkcc_validate(const float *__restrict__ q, Ctx &ctx)
+{
+    return fkcc(q, ctx);
+}
+
 // World centre and radius of every model sphere (model sphere order).
 __device__ __forceinline__ void fk_spheres(const float *__restrict__ q, float4 *__restrict__ out)
 {
