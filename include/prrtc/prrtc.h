@@ -313,10 +313,14 @@ typedef struct prrtc_smooth_settings {
     float cost_weight;     /* weight of dC/dq (100) */
     float smooth_weight;   /* weight of the discrete path Laplacian (1) */
     int granularity;       /* checker points per edge for the final judgement (128) */
+    int shortcut_rounds;   /* shortcut attempts before smoothing (8): a span (i, j) is replaced by
+                              evenly spaced points on the segment q_i -> q_j when its sub-edges
+                              are free at granularity / 4 points */
 } prrtc_smooth_settings;
 void prrtc_smooth_settings_default(prrtc_smooth_settings *s);
 
-/* Smooths paths in place: `steps` iterations of
+/* Shortens and smooths paths in place: `shortcut_rounds` shortcut attempts,
+ * then `steps` iterations of
  *   q_w -= step * (cost_weight * dC/dq(q_w) + smooth_weight * (2 q_w - q_{w-1} - q_{w+1}))
  * on the interior waypoints (end points fixed, joint limits clamped), then
  * checks every edge with the collision checker at `granularity` points

@@ -97,7 +97,7 @@ class BatchSettings(C.Structure):
 class SmoothSettings(C.Structure):
     """prrtc_smooth_settings."""
     _fields_ = [("margin", C.c_float), ("steps", C.c_int), ("step", C.c_float), ("cost_weight", C.c_float),
-                ("smooth_weight", C.c_float), ("granularity", C.c_int)]
+                ("smooth_weight", C.c_float), ("granularity", C.c_int), ("shortcut_rounds", C.c_int)]
 
     def __init__(self, **kw):
         super().__init__()

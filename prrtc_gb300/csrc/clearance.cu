@@ -221,6 +221,7 @@ extern "C" void prrtc_smooth_settings_default(prrtc_smooth_settings *s)
     s->cost_weight = 100.0f;
     s->smooth_weight = 1.0f;
     s->granularity = 128;
+    s->shortcut_rounds = 8;
 }
 
 extern "C" prrtc_status prrtc_smooth_paths(prrtc_ctx *ctx, prrtc_robot robot, const prrtc_env *const *envs,
@@ -235,7 +236,7 @@ extern "C" prrtc_status prrtc_smooth_paths(prrtc_ctx *ctx, prrtc_robot robot, co
         return c->fail(PRRTC_EINVAL, "smooth_paths: bad argument (2 <= waypoints <= 256)");
     const prrtc_smooth_settings &st = *settings;
     if (!(st.margin >= 0.0f) || st.steps < 0 || !(st.step >= 0.0f) || !(st.cost_weight >= 0.0f) ||
-        !(st.smooth_weight >= 0.0f) || st.granularity < 1 || st.granularity > (1 << 20))
+        !(st.smooth_weight >= 0.0f) || st.granularity < 1 || st.granularity > (1 << 20) || st.shortcut_rounds < 0)
         return c->fail(PRRTC_EINVAL, "smooth_paths: bad settings");
     if (n_paths == 0) return PRRTC_OK;
     std::lock_guard<std::mutex> g(c->mu);
@@ -261,7 +262,7 @@ extern "C" prrtc_status prrtc_smooth_paths(prrtc_ctx *ctx, prrtc_robot robot, co
     P.n_paths = n_paths;
     P.waypoints = waypoints;
     P.q = (float *)dq;
-    P.s = ClrSmooth{st.margin, st.step, st.cost_weight, st.smooth_weight, st.steps, st.granularity};
+    P.s = ClrSmooth{st.margin, st.step, st.cost_weight, st.smooth_weight, st.steps, st.granularity, st.shortcut_rounds};
     P.accepted = (uint8_t *)dacc;
     P.cost_before = (float *)dcb;
     P.cost_after = (float *)dca;

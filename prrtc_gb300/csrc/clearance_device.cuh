@@ -58,7 +58,7 @@ struct ClrEnv {
 // Smoothing settings as the kernels read them (prrtc_smooth_settings).
 struct ClrSmooth {
     float margin, step, cost_weight, smooth_weight;
-    int steps, granularity;
+    int steps, granularity, shortcut_rounds;
 };
 
 // One launch of the smoothing kernel over n_paths paths of `waypoints` rows.

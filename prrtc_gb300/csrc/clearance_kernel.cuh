@@ -3,6 +3,7 @@
 #pragma once
 
 #include "clearance_device.cuh"
+#include "planner_device.cuh"
 
 namespace prrtc {
 
@@ -19,8 +20,12 @@ __device__ __forceinline__ float block_sum(float v, float *s_red)
     return t;
 }
 
-// One block per path.  The path stays in shared memory for all `steps`
-// iterations of
+// One block per path.  First `shortcut_rounds` shortcut attempts: a span
+// (i, j) of the path, chosen by a hash of (path, round), is replaced by evenly
+// spaced points on the straight segment q_i -> q_j when every one of those
+// sub-edges is free at granularity / 4 points (a quick filter; the judge below
+// checks at full resolution).  Then the path stays in shared memory for all
+// `steps` iterations of
 //     q_w <- clamp(q_w - step * (cost_weight * dC/dq(q_w) + smooth_weight * (2 q_w - q_{w-1} - q_{w+1})))
 // over the interior waypoints (the end points stay where they are).  The
 // result is then checked edge by edge with the robot's checker at
@@ -46,6 +51,46 @@ __global__ void __launch_bounds__(128) k_smooth_paths(const ClrLaunch P)
     __syncthreads();
     const ClrEnv e{s_dyn, pe.n};
     const ClrSmooth s = P.s;
+    CheckCtx ctx{EnvView{e.rec, e.n}, 0.0f, &s_bad};
+    if (P.cost_before) {   // the cost of the path as given
+        float cost = 0.0f;
+        for (int w = threadIdx.x; w < W; w += blockDim.x) {
+            float g[kClrMaxJoints];
+            cost += clr::cost_grad(P.M, e, s_q + w * D, s.margin, s.cost_weight, g);
+        }
+        const float total = block_sum(cost, s_red);
+        if (threadIdx.x == 0) P.cost_before[path] = total;
+    }
+    const int gs = max(1, s.granularity / 4);
+    for (int r = 0; r < s.shortcut_rounds && W > 2; r++) {
+        const unsigned h = hash32((unsigned)path * 0x9E3779B1u + (unsigned)r * 0x85EBCA77u + 0x27D4EB2Fu);
+        const int span = 2 + (int)(h % (unsigned)min(W - 2, 31));   // 2 .. min(W - 1, 32) segments
+        const int i0 = (int)((h >> 8) % (unsigned)(W - span));
+        const float *qa = s_q + i0 * D, *qb = s_q + (i0 + span) * D;
+        if (threadIdx.x == 0) s_bad = 0;
+        __syncthreads();
+        // sub-edge m runs from p_m to p_{m+1}, p_m = qa + (m / span) (qb - qa)
+        for (int idx = threadIdx.x; idx < span * gs; idx += blockDim.x) {
+            if (*(volatile int *)&s_bad) break;
+            const int m = idx / gs, k = idx - m * gs + 1;
+            float cfg[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) {
+                const float delta = qb[d] - qa[d];
+                const float a = qa[d] + ((float)m / (float)span) * delta, b = qa[d] + ((float)(m + 1) / (float)span) * delta;
+                cfg[d] = __fadd_rn(a, __fmul_rn((float)k, __fdiv_rn(__fsub_rn(b, a), (float)gs)));
+            }
+            ctx.work = 0;
+            if (!Gen::fkcc(cfg, ctx)) s_bad = 1;
+        }
+        __syncthreads();
+        if (s_bad == 0)
+            for (int i = threadIdx.x; i < (span - 1) * D; i += blockDim.x) {
+                const int m = i / D + 1, d = i - (m - 1) * D;
+                s_q[(i0 + m) * D + d] = qa[d] + ((float)m / (float)span) * (qb[d] - qa[d]);
+            }
+        __syncthreads();
+    }
     for (int it = 0; it <= s.steps; it++) {
         float cost = 0.0f;
         for (int w = threadIdx.x; w < W; w += blockDim.x) {
@@ -57,12 +102,9 @@ __global__ void __launch_bounds__(128) k_smooth_paths(const ClrLaunch P)
                     s_g[w * D + d] =
                         g[d] + s.smooth_weight * (2.0f * s_q[w * D + d] - s_q[(w - 1) * D + d] - s_q[(w + 1) * D + d]);
         }
-        if (it == 0 || it == s.steps) {
+        if (it == s.steps) {
             const float total = block_sum(cost, s_red);
-            if (threadIdx.x == 0) {
-                float *out = it == 0 ? P.cost_before : P.cost_after;
-                if (out) out[path] = total;
-            }
+            if (threadIdx.x == 0 && P.cost_after) P.cost_after[path] = total;
         }
         __syncthreads();
         if (it == s.steps) break;
@@ -75,7 +117,6 @@ __global__ void __launch_bounds__(128) k_smooth_paths(const ClrLaunch P)
     // the judge: every edge at the planner's interpolation points
     if (threadIdx.x == 0) s_bad = 0;
     __syncthreads();
-    CheckCtx ctx{EnvView{e.rec, e.n}, 0.0f, &s_bad};
     const float fg = (float)s.granularity;
     const int total = (W - 1) * s.granularity;
     for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {

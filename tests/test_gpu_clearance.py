@@ -203,3 +203,20 @@ def test_autograd_shim_descent(ctx, oracle, planned):
     ok = [oracle.check_edges("panda", e, out[i, :-1], out[i, 1:], 128).all() for i, e in enumerate(envs)]
     assert np.mean(ok) >= 0.5
     assert cost_fn(x.detach()).sum().item() < cost_fn(torch.from_numpy(P).cuda()).sum().item()
+
+
+def test_shortcuts_alone(ctx, oracle, planned):
+    """Shortcut attempts only (no gradient steps): every accepted path is
+    clean under the oracle at 128 points per edge, keeps its end points and
+    is no longer than before; most paths get shorter."""
+    from prrtc_gb300 import SmoothSettings, paths
+    envs, P = planned["panda"]
+    out, acc, _, _ = ctx.smooth_paths("panda", envs, P, SmoothSettings(steps=0, shortcut_rounds=64))
+    a = acc.astype(bool)
+    assert a.mean() >= 0.5, a.mean()
+    for i in np.flatnonzero(a):
+        assert oracle.check_edges("panda", envs[i], out[i, :-1], out[i, 1:], 128).all(), i
+        np.testing.assert_array_equal(out[i, [0, -1]], P[i, [0, -1]])
+    before, after = paths.length(P[a]), paths.length(out[a])
+    assert (after <= before * (1 + 1e-5)).all()
+    assert (after < before * 0.99).mean() >= 0.5
