@@ -189,6 +189,19 @@ prrtc_status prrtc_validate_edges(prrtc_ctx *ctx, prrtc_robot robot, const prrtc
  */
 prrtc_status prrtc_validate_configs_noalloc(prrtc_robot robot, const prrtc_env_desc *env, const float *q,
                                             int64_t n, uint8_t *out_free, void *stream);
+/*
+ * Goal regions (no counterpart in pRRTC, whose goals are configurations,
+ * pRRTC.cu:690-693): up to max_goals collision-free configurations whose model
+ * sphere `sphere` (e.g. the hand's bounding sphere) has its centre inside the
+ * box [box_lo, box_hi] (world, metres).  Candidates t = 0 .. tries-1 of a
+ * seeded sequence spanning the joint box are tested on the GPU; the first
+ * accepted ones in sequence order are returned, so the result depends only
+ * on the arguments.  goals: host [max_goals][dof]; *num_found receives the
+ * count.  Pass them as a query's goals (num_goals > 1 is a goal set).
+ */
+prrtc_status prrtc_sample_goals(prrtc_ctx *ctx, prrtc_robot robot, const prrtc_env *env, int sphere,
+                                const float *box_lo, const float *box_hi, uint64_t seed, int64_t tries,
+                                int max_goals, float *goals, int *num_found);
 /* World centre and radius of every model sphere: out is [n][num_spheres][4]. */
 prrtc_status prrtc_fk_spheres(prrtc_ctx *ctx, prrtc_robot robot, const float *q, int64_t n,
                               float *out);

@@ -153,6 +153,8 @@ def lib():
             "prrtc_validate_configs": (C.c_int, [vp, C.c_int, vp, fp, i64, u8p]),
             "prrtc_validate_edges": (C.c_int, [vp, C.c_int, vp, fp, fp, i64, C.c_int, u8p]),
             "prrtc_fk_spheres": (C.c_int, [vp, C.c_int, fp, i64, fp]),
+            "prrtc_sample_goals": (C.c_int, [vp, C.c_int, vp, C.c_int, fp, fp, C.c_uint64, i64, C.c_int, fp,
+                                             C.POINTER(C.c_int)]),
             "prrtc_settings_default": (None, [C.POINTER(Settings)]),
             "prrtc_solve": (C.c_int, [vp, C.c_int, fp, fp, C.c_int, vp, C.POINTER(Settings), C.POINTER(_Result)]),
             "prrtc_measure_fp32_peak": (C.c_int, [vp, C.POINTER(C.c_double)]),
@@ -300,6 +302,21 @@ class Context:
         po, ko = _ptr(out)
         self._check(lib().prrtc_validate_edges(self.handle, rid, e.handle, pa, pb, n, int(granularity), po))
         return out
+
+    def sample_goals(self, robot, env, sphere: int, box_lo, box_hi, max_goals: int = 8, tries: int = 1 << 20,
+                     seed: int = 0) -> np.ndarray:
+        """[k, dof] collision-free configurations (k <= max_goals) whose model
+        sphere `sphere` has its centre inside the box (prrtc_sample_goals)."""
+        rid = robot_id(robot)
+        e = self._env(env)
+        lo = np.ascontiguousarray(np.asarray(box_lo, np.float32).reshape(3))
+        hi = np.ascontiguousarray(np.asarray(box_hi, np.float32).reshape(3))
+        out = np.empty((max(max_goals, 1), dof(rid)), np.float32)
+        k = C.c_int()
+        self._check(lib().prrtc_sample_goals(self.handle, rid, e.handle, int(sphere), C.c_void_p(lo.ctypes.data),
+                                             C.c_void_p(hi.ctypes.data), int(seed), int(tries), int(max_goals),
+                                             C.c_void_p(out.ctypes.data), C.byref(k)))
+        return out[:k.value].copy()
 
     def fk_spheres(self, robot, q):
         """[n, num_spheres, 4] world centres and radii."""

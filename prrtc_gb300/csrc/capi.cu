@@ -323,6 +323,49 @@ prrtc_status prrtc_validate_configs(prrtc_ctx *ctx, prrtc_robot robot, const prr
     return c->cuda(cudaStreamSynchronize(c->stream), "validate_configs");
 }
 
+prrtc_status prrtc_sample_goals(prrtc_ctx *ctx, prrtc_robot robot, const prrtc_env *env, int sphere,
+                                const float *box_lo, const float *box_hi, uint64_t seed, int64_t tries, int max_goals,
+                                float *goals, int *num_found)
+{
+    Ctx *c = Ctx::of(ctx);
+    const RobotOps *ops = robot_ops(robot);
+    const Env *e = reinterpret_cast<const Env *>(env);
+    if (!c) return PRRTC_EINVAL;
+    if (!ops || !e || !box_lo || !box_hi || !num_found || tries < 0 || max_goals < 0 || (max_goals > 0 && !goals) ||
+        sphere < 0 || sphere >= ops->num_spheres)
+        return c->fail(PRRTC_EINVAL, "sample_goals: bad argument");
+    if (tries > (int64_t)1 << 30) return c->fail(PRRTC_EINVAL, "sample_goals: at most 2^30 tries per call");
+    *num_found = 0;
+    if (tries == 0 || max_goals == 0) return PRRTC_OK;
+    std::lock_guard<std::mutex> g(c->mu);
+    cudaSetDevice(c->device);
+    GoalQuery gq{};
+    gq.seed = seed;
+    gq.tries = tries;
+    gq.sphere = sphere;
+    for (int k = 0; k < 3; k++) {
+        gq.lo[k] = box_lo[k];
+        gq.hi[k] = box_hi[k];
+    }
+    prrtc_robot_limits(robot, gq.scale, gq.offset);
+    uint8_t *flags = static_cast<uint8_t *>(c->scratch(1, (size_t)tries));
+    if (!flags) return c->fail(PRRTC_ENOMEM, "sample_goals: %lld flags", (long long)tries);
+    LaunchEnv le{e->dev, e->counts, c->sms, nullptr};
+    prrtc_status s;
+    if ((s = c->cuda(ops->goal_flags(le, gq, flags, c->stream), "sample_goals launch"))) return s;
+    c->launches++;
+    std::vector<uint8_t> h((size_t)tries);
+    if ((s = c->cuda(cudaMemcpyAsync(h.data(), flags, (size_t)tries, cudaMemcpyDeviceToHost, c->stream), "sample_goals copy")) ||
+        (s = c->cuda(cudaStreamSynchronize(c->stream), "sample_goals")))
+        return s;
+    // the first max_goals accepted candidates, in candidate order (deterministic)
+    int found = 0;
+    for (int64_t t = 0; t < tries && found < max_goals; t++)
+        if (h[(size_t)t]) goal_candidate(seed, t, ops->dof, gq.scale, gq.offset, goals + (size_t)found++ * ops->dof);
+    *num_found = found;
+    return PRRTC_OK;
+}
+
 prrtc_status prrtc_validate_edges(prrtc_ctx *ctx, prrtc_robot robot, const prrtc_env *env, const float *a,
                                   const float *b, int64_t n, int granularity, uint8_t *out_free)
 {

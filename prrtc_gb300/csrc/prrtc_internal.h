@@ -149,6 +149,39 @@ struct BatchParams {
     float scale[16], offset[16];
 };
 
+// Goal-region sampling (prrtc_sample_goals): candidate t of a seed, the same
+// on the host and the device (integer hash, then one correctly rounded fmaf
+// per joint), so the host can rebuild the candidates the device accepted.
+__host__ __device__ inline unsigned goal_hash(unsigned x)
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+__host__ __device__ inline void goal_candidate(unsigned long long seed, long long t, int dof, const float *scale,
+                                               const float *offset, float *q)
+{
+    for (int d = 0; d < dof; d++) {
+        unsigned h = goal_hash((unsigned)seed ^ goal_hash((unsigned)(seed >> 32) + 0x9E3779B9u * (unsigned)d));
+        h = goal_hash(h ^ (unsigned)t);
+        h = goal_hash(h ^ (unsigned)((unsigned long long)t >> 32) ^ 0x85EBCA6Bu);
+        const float u = (float)(h >> 8) * (1.0f / 16777216.0f);   // [0, 1), 24 bits, exact
+        q[d] = fmaf(u, scale[d], offset[d]);
+    }
+}
+
+struct GoalQuery {
+    unsigned long long seed;
+    long long tries;
+    int sphere;                   // model sphere whose centre must lie in the box
+    float lo[3], hi[3];
+    float scale[16], offset[16];  // the robot's joint box
+};
+
 struct ClrLaunch;   // clearance_device.cuh
 struct Ctx;         // context.h
 
@@ -168,6 +201,7 @@ struct RobotOps {
     cudaError_t (*solve_batch)(const BatchParams &, int blocks, int warps_per_block, cudaStream_t);
     int (*batch_occupancy)(int warps_per_block);   // resident blocks per SM
     cudaError_t (*smooth_paths)(const ClrLaunch &, size_t env_bytes, cudaStream_t);
+    cudaError_t (*goal_flags)(const LaunchEnv &, const GoalQuery &, uint8_t *flags, cudaStream_t);
 };
 
 // Shuffled Halton prime bases per sampling lane, as the reference seeds them

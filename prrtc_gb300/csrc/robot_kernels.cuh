@@ -96,6 +96,32 @@ __global__ void __launch_bounds__(128) k_validate_edges(const float4 *__restrict
     add_work(work, flops, cfgs);
 }
 
+// Goal-region candidates: flags[t] = 1 when candidate t (goal_candidate)
+// puts the chosen sphere's centre in the box and the checker finds it free.
+template <class Gen>
+__global__ void __launch_bounds__(128) k_goal_flags(const float4 *__restrict__ env, EnvCounts nc, const GoalQuery g,
+                                                    uint8_t *__restrict__ flags)
+{
+    extern __shared__ float4 s_env[];
+    stage_env(s_env, env, nc.records());
+    __syncthreads();
+    CheckCtx ctx{{s_env, nc}, 0.0f, nullptr};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < g.tries; t += (long long)gridDim.x * blockDim.x) {
+        float q[Gen::kDof];
+        goal_candidate(g.seed, t, Gen::kDof, g.scale, g.offset, q);
+        float4 s[Gen::kNumSpheres];
+        Gen::fk_spheres(q, s);
+        const float4 c = s[g.sphere];
+        bool ok = c.x >= g.lo[0] && c.x <= g.hi[0] && c.y >= g.lo[1] && c.y <= g.hi[1] && c.z >= g.lo[2] &&
+                  c.z <= g.hi[2];
+        if (ok) {
+            ctx.work = 0;
+            ok = Gen::fkcc_validate(q, ctx);
+        }
+        flags[t] = ok ? 1 : 0;
+    }
+}
+
 template <class Gen>
 __global__ void __launch_bounds__(128) k_fk_spheres(const float *__restrict__ q, int64_t n, float4 *__restrict__ out)
 {
@@ -391,6 +417,13 @@ struct RobotKernels {
         }
         return n;
     }
+    static cudaError_t goal_flags(const LaunchEnv &le, const GoalQuery &g, uint8_t *flags, cudaStream_t st)
+    {
+        if (g.tries <= 0) return cudaSuccess;
+        const size_t smem = (size_t)le.counts.records() * sizeof(float4);
+        k_goal_flags<Gen><<<grid_for(g.tries, 128, le.sms, 16), 128, smem, st>>>(le.rec, le.counts, g, flags);
+        return cudaGetLastError();
+    }
     static cudaError_t smooth_paths(const ClrLaunch &P, size_t env_bytes, cudaStream_t st)
     {
         if (P.n_paths <= 0) return cudaSuccess;
@@ -413,6 +446,7 @@ struct RobotKernels {
         o.solve_batch = &solve_batch;
         o.batch_occupancy = &batch_occupancy;
         o.smooth_paths = &smooth_paths;
+        o.goal_flags = &goal_flags;
         (void)dof_check;
         return o;
     }
