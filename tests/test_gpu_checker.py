@@ -115,3 +115,31 @@ def test_work_counts_match_oracle(case, ctx, oracle):
     fk = 2 * (12 * m["dof"] + 9 * len(m["spheres"]))
     assert n == len(q)
     assert flops == int(counts @ WEIGHTS) + fk * len(q)
+
+
+def test_maximum_environment_and_zero_length_edges(ctx, oracle):
+    """A scene of exactly PRRTC_MAX_ENV_FLOATS packed floats (all obstacle
+    types) checks like the oracle, outside the near-contact bucket; an edge
+    from a configuration to itself checks that configuration."""
+    from prrtc_gb300 import scenes
+    from prrtc_gb300.env import Environment, capsule_row, cuboid_row
+    rng = np.random.default_rng(5)
+
+    def pos(n):
+        return rng.uniform([0.3, -0.8, 0.0], [1.3, 0.8, 1.4], (n, 3))
+
+    sph = np.column_stack([pos(256), rng.uniform(0.01, 0.04, 256)]).astype(np.float32)          # 1024 floats
+    caps = np.array([capsule_row(p, p + rng.uniform(-0.1, 0.1, 3), rng.uniform(0.01, 0.03)) for p in pos(256)])  # 2048
+    cubs = np.array([cuboid_row(p, rng.uniform(0.01, 0.05, 3), rng.uniform(-1, 1, 3)) for p in pos(512)])       # 8192
+    env = Environment(spheres=sph, capsules=caps, cuboids=cubs)
+    assert env.packed_floats() == 11264
+    q = scenes._uniform_configs("panda", scenes.Rng(9), 20000).astype(np.float32)
+    got = ctx.validate_configs("panda", env, q)
+    ref, margin = oracle.check("panda", env, q, margin=True)
+    bad = np.flatnonzero(got != ref)
+    assert (margin[bad] < 1e-5).all(), margin[bad]
+    free = q[ref == 1][:64]
+    assert len(free) > 0
+    same = ctx.validate_edges("panda", env, free, free, 32)
+    np.testing.assert_array_equal(same, oracle.check_edges("panda", env, free, free, 32))
+    assert same.all()
