@@ -391,45 +391,51 @@ class Context:
         return Batch(self, robot, queries, settings if settings is not None else BatchSettings(), path_capacity)
 
     def solve_batch(self, robot, queries, settings: BatchSettings | None = None, path_capacity: int = 4096) -> list:
-        """prrtc_solve_batch: upload, solve and download in one call."""
+        """prrtc_solve_batch: upload, solve and download in one call.  The
+        query, descriptor and result arrays are built as numpy arrays with the
+        C structs' layouts (no per-query ctypes work)."""
         rid = robot_id(robot)
-        b = Batch.__new__(Batch)
-        b.ctx, b.rid, b.D, b.n, b.path_capacity = self, rid, dof(rid), len(queries), path_capacity
-        b.handle = None
-        keep = []
-        qs = (_Query * b.n)()
+        D, n = dof(rid), len(queries)
         trip = [q if isinstance(q, tuple) else (q.env, q.start, q.goal) for q in queries]
-        # every start and goal in two contiguous arrays; each query points into them
-        starts = np.ascontiguousarray(np.stack([np.asarray(s, np.float32).reshape(b.D) for _, s, _ in trip]))
-        goal_list = [np.asarray(g, np.float32).reshape(-1, b.D) for _, _, g in trip]
+        starts = np.ascontiguousarray(np.stack([np.asarray(s, np.float32).reshape(D) for _, s, _ in trip]))
+        goal_list = [np.asarray(g, np.float32).reshape(-1, D) for _, _, g in trip]
         goals = np.ascontiguousarray(np.concatenate(goal_list))
-        keep += [starts, goals]
-        s0, g0, row = starts.ctypes.data, goals.ctypes.data, 4 * b.D
-        descs = (EnvDesc * b.n)()
-        d0, dsz = C.addressof(descs), C.sizeof(EnvDesc)
-        keep.append(descs)
-        goff = 0
-        for i, (env, _, _) in enumerate(trip):
-            if isinstance(env, EnvHandle):
-                qs[i].env = env.handle
-            else:
-                d, k = _env_desc(env)
-                descs[i] = d
-                keep.append(k)
-                qs[i].env_desc = d0 + i * dsz
-            ng = len(goal_list[i])
-            qs[i].start, qs[i].goals, qs[i].num_goals = s0 + i * row, g0 + goff * row, ng
-            goff += ng
-        res = (_Result * b.n)()
-        paths = np.empty((b.n, path_capacity, b.D), np.float32)
-        for i in range(b.n):
-            res[i].path_capacity = path_capacity
-            res[i].path = paths[i].ctypes.data_as(C.POINTER(C.c_float))
+        ngoals = np.fromiter((len(g) for g in goal_list), np.int64, n)
+        qs = np.zeros(n, _QUERY_DT)
+        qs["start"] = starts.ctypes.data + 4 * D * np.arange(n, dtype=np.uint64)
+        qs["goals"] = goals.ctypes.data + 4 * D * (np.cumsum(ngoals) - ngoals).astype(np.uint64)
+        qs["num_goals"] = ngoals
+        keep = [starts, goals]
+        is_handle = np.fromiter((isinstance(e, EnvHandle) for e, _, _ in trip), bool, n)
+        if is_handle.any():
+            qs["env"][is_handle] = [e.handle.value for (e, _, _), h in zip(trip, is_handle) if h]
+        plain = np.flatnonzero(~is_handle)
+        if len(plain):
+            descs = np.zeros(len(plain), _DESC_DT)
+            for k in _ENV_KINDS:                       # one buffer per obstacle type, descriptors point into it
+                arrs = [np.asarray(getattr(trip[i][0], k), np.float32) for i in plain]
+                cnt = np.fromiter((len(a) for a in arrs), np.int64, len(arrs))
+                if cnt.sum():
+                    buf = np.ascontiguousarray(np.concatenate(arrs))
+                    keep.append(buf)
+                    ptr = buf.ctypes.data + (buf.shape[1] * 4 * (np.cumsum(cnt) - cnt)).astype(np.uint64)
+                    descs[k] = np.where(cnt > 0, ptr, 0)
+                descs["num_" + k] = cnt
+            keep.append(descs)
+            qs["env_desc"][plain] = descs.ctypes.data + _DESC_DT.itemsize * np.arange(len(plain), dtype=np.uint64)
+        paths = np.empty((n, path_capacity, D), np.float32)
+        res = np.zeros(n, _RESULT_DT)
+        res["path_capacity"] = path_capacity
+        res["path"] = paths.ctypes.data + 4 * D * path_capacity * np.arange(n, dtype=np.uint64)
         s = settings if settings is not None else BatchSettings()
-        self._check(lib().prrtc_solve_batch(self.handle, rid, qs, b.n, C.byref(s), res))
-        return [PlannerResult(bool(r.solved), paths[i, :r.path_rows].copy(), r.start_tree_size, r.goal_tree_size,
-                              r.path_length, r.iters, r.cost, r.wall_ns, r.kernel_ns, r.copy_ns, r.status)
-                for i, r in enumerate(res)]
+        self._check(lib().prrtc_solve_batch(self.handle, rid, C.cast(C.c_void_p(qs.ctypes.data), C.POINTER(_Query)), n,
+                                            C.byref(s), C.cast(C.c_void_p(res.ctypes.data), C.POINTER(_Result))))
+        cols = {f: res[f].tolist() for f in ("solved", "path_rows", "start_tree_size", "goal_tree_size", "path_length",
+                                             "iters", "cost", "wall_ns", "kernel_ns", "copy_ns", "status")}
+        return [PlannerResult(bool(cols["solved"][i]), paths[i, :cols["path_rows"][i]].copy(), cols["start_tree_size"][i],
+                              cols["goal_tree_size"][i], cols["path_length"][i], cols["iters"][i], cols["cost"][i],
+                              cols["wall_ns"][i], cols["kernel_ns"][i], cols["copy_ns"][i], cols["status"][i])
+                for i in range(n)]
 
     def solve(self, robot, start, goals, env, settings: Settings | None = None, path_capacity: int = 70000) -> PlannerResult:
         """pRRTC::solve<Robot>(start, goals, env, settings)."""
@@ -519,6 +525,17 @@ class Batch:
 _ENV_KINDS = ("spheres", "capsules", "z_aligned_capsules", "cylinders", "cuboids", "z_aligned_cuboids")
 
 
+def _numpy_dtype(struct) -> np.dtype:
+    """A numpy structured dtype with a ctypes struct's field layout."""
+    kinds = {C.c_void_p: "u8", C.c_int: "i4", C.c_uint32: "u4", C.c_uint64: "u8", C.c_int64: "i8", C.c_float: "f4"}
+    names, formats, offsets = [], [], []
+    for name, ctype in struct._fields_:
+        names.append(name)
+        offsets.append(getattr(struct, name).offset)
+        formats.append("u8" if issubclass(ctype, C._Pointer) else kinds[ctype])
+    return np.dtype({"names": names, "formats": formats, "offsets": offsets, "itemsize": C.sizeof(struct)})
+
+
 def _env_desc(env: Environment):
     keep, args = [], []
     for k in _ENV_KINDS:
@@ -534,3 +551,8 @@ def _env_desc(env: Environment):
 def _empty_like_device(t, shape, dtype: str):
     import torch
     return torch.empty(shape, dtype=getattr(torch, dtype), device=t.device)
+
+
+_QUERY_DT = _numpy_dtype(_Query)
+_DESC_DT = _numpy_dtype(EnvDesc)
+_RESULT_DT = _numpy_dtype(_Result)
