@@ -274,7 +274,9 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     P.restart_after_ns = settings->restart_after_ns ? settings->restart_after_ns : 10000000ull;
     // pRRTC stops a query when any of its num_new_configs lanes passes max_iters
     // (pRRTC.cu:343-346), i.e. after about max_iters x num_new_configs samples
-    P.max_samples_drawn = std::min<long long>((long long)S.max_iters * S.num_new_configs, 0x7fffffffLL);
+    // below 2^31 with room for the tickets that warps take after the last one
+    // (32 per warp per round): sample indices and Halton indices stay int
+    P.max_samples_drawn = std::min<long long>((long long)S.max_iters * S.num_new_configs, kMaxSamplesDrawn);
     P.cfg_pool = reinterpret_cast<const float *>(base + o_cfg);
     P.queries = reinterpret_cast<const BatchQueryDesc *>(base + o_desc);
     P.qstate = reinterpret_cast<QueryState *>(base + o_qstate);

@@ -35,9 +35,147 @@ struct WarpScratch {
     float4 env[kWarpEnvRecords];
     float from[16], step[16], cfg[16], nn[16], vec[16], next[16];
     float chunk[16][33];   // 32 tree nodes staged for the round's nearest-neighbour pass (+1: bank skew)
+    float dom[7][33];      // early rejection: the first coordinates of a small tree's nodes,
+    float rad2[32];        // their squared widened domain radii
+    float box_lo[8], box_hi[8];   // and the box around all their domains
+    unsigned hsh[16];      // scrambled sampler: the hash of (query, attempt, dimension)
     int bad;
     int pad_[3];
 };
+
+// Exact early rejection of dynamic-domain samples.  When every lane of a
+// round samples the same tree and it has at most 32 nodes (a trapped tree
+// rejects all but ~1e-4 of its samples), the nodes are staged with their
+// domain radii widened by kEarlyRel and kEarlyAbs (float rounding of the
+// full test stays far inside that), and the digit loops stop after
+// kEarlyTrips trips: each coordinate of the first dimension group is then
+// known to an interval.  A lane whose interval box is outside every widened
+// domain would be rejected by the full test whatever its remaining digits
+// are; when that holds for every lane, the warp skips the rest of the
+// round.  Otherwise the digit loops continue from where they stopped, so
+// samples and decisions are the same as without the test.  The nodes are
+// staged every round, as the full test reads them; a tree of more than
+// kEarlyBox nodes also gets the box around all its domains as a first test.
+constexpr int kEarlyTrips = 4;
+constexpr float kEarlyRel = 1.0f / 1024.0f, kEarlyAbs = 1.0f / 65536.0f;
+constexpr int kEarlyBox = 8;
+
+// whole warp: stage the first G coordinates and the widened radii of the
+// tree's first cnt (<= 32) nodes and, above kEarlyBox nodes, the box around
+// their domains.  A node with a NaN coordinate or radius (an insertion in
+// flight) makes the box unbounded in that dimension.
+template <int G>
+__device__ __forceinline__ void stage_domains(WarpScratch &W, const float *nd, const float *rd, int cap, int cnt)
+{
+    const int lane = lane_id();
+    const bool have = lane < cnt;
+    const float r = have ? __ldcg(rd + lane) : 0.0f;
+    const float m = fmaf(r, 1.0f + kEarlyRel, kEarlyAbs);
+    W.rad2[lane] = m * m;
+#pragma unroll
+    for (int j = 0; j < G; j++) {
+        const float c = have ? __ldcg(nd + (size_t)j * cap + lane) : 0.0f;
+        W.dom[j][lane] = c;
+        if (cnt <= kEarlyBox) continue;
+        float lo = c - m, hi = c + m;
+        if (!have) {
+            lo = INFINITY;
+            hi = -INFINITY;
+        } else if (!(lo == lo) || !(hi == hi)) {
+            lo = -INFINITY;
+            hi = INFINITY;
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, off));
+            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, off));
+        }
+        if (lane == 0) {
+            W.box_lo[j] = lo;
+            W.box_hi[j] = hi;
+        }
+    }
+    __syncwarp();
+}
+
+// one lane: can the sample whose first G coordinates are being digitised in
+// r still land in a staged domain?  The digits to come add less than
+// f * b to h (nothing once idx is 0), plus at most 2^-20 of rounding over
+// the remaining fmaf steps; the scrambled sampler's rotation keeps an
+// interval unless it wraps past 1.  Coordinates are fmaf(v, scale, offset),
+// monotone in v.  A NaN anywhere answers yes.
+template <int G, bool SCRAMBLE>
+__device__ __forceinline__ bool early_near(const RadicalDigits<G, SCRAMBLE> &r, const unsigned (&hsh)[G],
+                                           const BatchParams &P, const WarpScratch &W, int cnt)
+{
+    float lo[G], hi[G];
+    bool in_box = true;
+#pragma unroll
+    for (int j = 0; j < G; j++) {
+        const float w = r.idx[j] ? fmaf(r.f[j] * (float)r.b[j], 1.0f + kEarlyRel, 1.0f / 1048576.0f) : 0.0f;
+        float vlo = r.h[j], vhi = r.h[j] + w;
+        if (SCRAMBLE) {
+            const float rot = (float)(hsh[j] >> 8) * (1.0f / 16777216.0f);
+            vlo += rot;
+            vhi += rot;
+            if (vlo >= 1.0f) {
+                vlo -= 1.0f;
+                vhi -= 1.0f;
+            } else if (vhi >= 1.0f) {
+                vlo = 0.0f;
+                vhi = 1.0f;
+            }
+        }
+        const float qa = fmaf(vlo, P.scale[j], P.offset[j]), qb = fmaf(vhi, P.scale[j], P.offset[j]);
+        lo[j] = fminf(qa, qb);
+        hi[j] = fmaxf(qa, qb);
+        if (cnt > kEarlyBox) in_box = in_box && !(hi[j] < W.box_lo[j] || lo[j] > W.box_hi[j]);
+    }
+    bool near = false;
+    if (in_box) {
+        for (int n = 0; n < cnt && !near; n++) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int j = 0; j < G; j++) {
+                const float c = W.dom[j][n];
+                const float g = fmaxf(fmaxf(c - hi[j], lo[j] - c), 0.0f);
+                acc = fmaf(g, g, acc);
+            }
+            near = !(acc > W.rad2[n]);
+        }
+    }
+    return near;
+}
+
+// whole warp: the coordinates d0 .. d0 + G - 1 of every lane's sample into
+// qv.  With `early` (first group only), returns true when the early test
+// rejected every lane's sample; qv is then incomplete.
+template <int D, int G, bool SCRAMBLE>
+__device__ __forceinline__ bool sample_group(const BatchParams &P, const WarpScratch &W, unsigned iter, int d0,
+                                             const unsigned (&bs)[G], const unsigned (&as)[G],
+                                             const unsigned (&hsh)[G], bool early, int cnt, bool valid, float (&qv)[D])
+{
+    RadicalDigits<G, SCRAMBLE> r(iter, bs, as);
+    if (early) {
+        r.run(kEarlyTrips);
+        const bool near = valid && early_near<G, SCRAMBLE>(r, hsh, P, W, cnt);
+        if (!__any_sync(0xffffffffu, near)) return true;
+    }
+    r.finish();
+#pragma unroll
+    for (int j = 0; j < G; j++) {
+        const int d = d0 + j;
+        if (d < D) {
+            float h = r.h[j];
+            if (SCRAMBLE) {
+                h += (float)(hsh[j] >> 8) * (1.0f / 16777216.0f);
+                h -= floorf(h);
+            }
+            qv[d] = fmaf(h, P.scale[d], P.offset[d]);
+        }
+    }
+    return false;
+}
 
 // Whole warp: check the g points of the edge in W (from + k * step),
 // k = 1..g, in ceil(g / 32) rounds of one point per lane.  Contiguous order
@@ -363,8 +501,15 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
     const int lane = lane_id();
     BatchCounters *C = P.ctr;
     const float fg = (float)P.granularity;
-    if (lane == 0) atomicCAS(&C->t0, 0ull, global_ns());
+    unsigned long long t0 = 0;   // lane 0: the launch's start (the first warp's clock)
+    if (lane == 0) {
+        const unsigned long long now = global_ns();
+        const unsigned long long first = atomicCAS(&C->t0, 0ull, now);
+        t0 = first ? first : now;
+    }
     int slot = -1;
+    int cq = 0, catt = 0;   // the slot's query and attempt, read when this warp takes the slot
+    bool fresh = true;
     unsigned idle = 0;
     const float4 *staged = nullptr;   // the global records now in W.env
     unsigned long long nn_visits = 0;   // flushed once per warp (a shared counter would serialise)
@@ -376,7 +521,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
     while (true) {
         // ---- time budget
         int timed_out = 0;
-        if (lane == 0 && P.budget_ns) timed_out = global_ns() - *(volatile unsigned long long *)&C->t0 > P.budget_ns;
+        if (lane == 0 && P.budget_ns) timed_out = global_ns() - t0 > P.budget_ns;
         timed_out = __shfl_sync(FULL, timed_out, 0);
         if (timed_out) {
             if (slot >= 0) {
@@ -456,6 +601,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                 if (att >= 0) {
                     batch_admit<D>(P, free_slot, qc, att);
                     slot = free_slot;
+                    fresh = true;
                     idle = 0;
                     continue;
                 }
@@ -463,6 +609,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
             if (rec >= 0) {
                 if (batch_leave<D>(P, rec, true)) {
                     slot = rec;
+                    fresh = true;
                     idle = 0;
                 }
                 continue;
@@ -484,6 +631,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
             }
             if (admit >= 0) batch_admit<D>(P, found, admit, 0);
             slot = found;
+            fresh = true;
             idle = 0;
         }
 
@@ -492,9 +640,24 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
         // nodes, and the samples that pass the dynamic-domain test are then
         // extended one at a time by the whole warp (32 of pRRTC's lanes
         // reading one tree snapshot, pRRTC.cu:378-427)
+        // The slot's query and attempt stay fixed while this warp works on it (a
+        // slot is reused only after its last worker has left).
         SlotState *S = &P.slots[slot];
-        const int q = vload(&S->query);
-        const int attempt = vload(&S->attempt);
+        if (fresh) {
+            if (lane == 0) {
+                cq = vload(&S->query);
+                catt = vload(&S->attempt);
+            }
+            cq = __shfl_sync(FULL, cq, 0);
+            catt = __shfl_sync(FULL, catt, 0);
+            // scrambled Halton: digit multiplier and rotation per (query, attempt, dimension)
+            if (lane < 16)
+                W.hsh[lane] = hash32((unsigned)cq * 0x9E3779B1u + (unsigned)catt * 0xC2B2AE35u +
+                                     (unsigned)lane * 0x85EBCA77u + 0x165667B1u);
+            __syncwarp();
+            fresh = false;
+        }
+        const int q = cq, attempt = catt;
         const BatchQueryDesc Qd = P.queries[q];
         const float4 *envp = Qd.env;
         if (Qd.env_n.records() <= kWarpEnvRecords) {
@@ -511,25 +674,42 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
         int *par_s = P.parents + (size_t)slot * 2 * P.cap;
         float *rad_s = P.radii + (size_t)slot * 2 * P.cap;
 
-        int k0 = 0, qdone = 0, f0 = 0, f1 = 0;
+        // the round's shared state in one batch of independent loads: the slot's
+        // and the query's states, the tree sizes and 32 sample tickets (taken
+        // even when the attempt turns out to have ended: a ticket is only a count)
+        int k0 = 0, sst = 0, qst = 0, f0 = 0, f1 = 0;
         if (lane == 0) {
-            qdone = vload(&P.qstate[q].state) == 2;
-            if (qdone) {
-                // another attempt finished the query: cancel this one
-                if (atomicCAS(&S->state, SLOT_RUNNING, SLOT_DONE) == SLOT_RUNNING) atomicSub(&P.qstate[q].live, 1);
-            } else {
-                k0 = atomicAdd(&S->ticket, 32);
-                f0 = vload(&S->free_index[0]);
-                f1 = vload(&S->free_index[1]);
-            }
+            sst = vload(&S->state);
+            qst = vload(&P.qstate[q].state);
+            f0 = vload(&S->free_index[0]);
+            f1 = vload(&S->free_index[1]);
+            k0 = atomicAdd(&S->ticket, 32);
         }
-        qdone = __shfl_sync(FULL, qdone, 0);
+        sst = __shfl_sync(FULL, sst, 0);
+        qst = __shfl_sync(FULL, qst, 0);
         k0 = __shfl_sync(FULL, k0, 0);
         f0 = __shfl_sync(FULL, f0, 0);
         f1 = __shfl_sync(FULL, f1, 0);
-        if (!qdone && (long long)k0 >= P.max_samples_drawn) {
+        if (sst != SLOT_RUNNING) {
+            // the attempt has ended (solved, failed or cancelled): leave the
+            // slot, possibly taking it over for a restart or the next query
+            if (batch_leave<D>(P, slot, true))
+                fresh = true;
+            else
+                slot = -1;
+            continue;
+        }
+        if (qst == 2) {
+            // another attempt finished the query: cancel this one
+            if (lane == 0 && atomicCAS(&S->state, SLOT_RUNNING, SLOT_DONE) == SLOT_RUNNING)
+                atomicSub(&P.qstate[q].live, 1);
+            continue;
+        }
+        if ((long long)k0 >= P.max_samples_drawn) {
             if (lane == 0) finish_attempt(P, S, q, 0);
-        } else if (!qdone) {
+            continue;
+        }
+        {
             // -- this lane's sample
             const int k = k0 + lane;
             const bool valid = (long long)k < P.max_samples_drawn;
@@ -558,199 +738,189 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
             float qv[D];
             // dimensions in ceil(D / 7) equal groups, each group's digit chains interleaved
             constexpr int NG = (D + 6) / 7, G = (D + NG - 1) / NG;
+            const int t0 = __shfl_sync(FULL, t, 0);
+            const int cnt0 = min(t0 == 0 ? f0 : f1, P.cap);
+            const bool early = P.dynamic_domain && cnt0 <= 32 && __all_sync(FULL, t == t0);
+            static_assert(G <= 7, "dimension groups of at most 7");
+            if (early)
+                stage_domains<G>(W, nodes_s + (size_t)t0 * D * P.cap, rad_s + (size_t)t0 * P.cap, P.cap, cnt0);
+            bool rejected = false;
 #pragma unroll
             for (int d0 = 0; d0 < D; d0 += G) {
                 unsigned bs[G], as[G], hsh[G];
-                float hv[G];
                 const int row = P.sampler == 0 ? (vl + attempt * P.lanes) % P.bases_lanes : vl % P.bases_lanes;
 #pragma unroll
                 for (int j = 0; j < G; j++) {
                     const int d = d0 + j < D ? d0 + j : D - 1;   // a short last group repeats a dimension
                     bs[j] = (unsigned)P.halton_bases[row * 16 + d];
-                    // scrambled Halton: digit multiplier and rotation per (query, attempt, dimension)
-                    hsh[j] = P.sampler == 0 ? 0u
-                                            : hash32((unsigned)q * 0x9E3779B1u + (unsigned)attempt * 0xC2B2AE35u +
-                                                     (unsigned)d * 0x85EBCA77u + 0x165667B1u);
+                    hsh[j] = P.sampler == 0 ? 0u : W.hsh[d];
                     as[j] = 1u + hsh[j] - div_by(hsh[j], kDivTable.magic[bs[j] - 1u]) * (bs[j] - 1u);
                 }
-                if (P.sampler == 0)
-                    radical_inverses<G, false>((unsigned)iter, bs, as, hv);
-                else
-                    radical_inverses<G, true>((unsigned)iter, bs, as, hv);
-#pragma unroll
-                for (int j = 0; j < G; j++) {
-                    const int d = d0 + j;
-                    if (d < D) {
-                        float h = hv[j];
-                        if (P.sampler != 0) {
-                            h += (float)(hsh[j] >> 8) * (1.0f / 16777216.0f);
-                            h -= floorf(h);
-                        }
-                        qv[d] = fmaf(h, P.scale[d], P.offset[d]);
-                    }
-                }
+                const bool e = early && d0 == 0;
+                const unsigned it = (unsigned)iter;
+                rejected = P.sampler == 0 ? sample_group<D, G, false>(P, W, it, d0, bs, as, hsh, e, cnt0, valid, qv)
+                                          : sample_group<D, G, true>(P, W, it, d0, bs, as, hsh, e, cnt0, valid, qv);
+                if (rejected) break;
             }
-            // -- nearest node of every lane's sample: one pass per tree, nodes
-            // staged 32 at a time in shared memory and read by all lanes
-            float best = FLT_MAX;
-            int bi = 0;
-            for (int tree = 0; tree < 2; tree++) {
-                if (!__any_sync(FULL, valid && t == tree)) continue;
-                const int cnt = min(tree == 0 ? f0 : f1, P.cap);
-                const float *nd = nodes_s + (size_t)tree * D * P.cap;
-                for (int base = 0; base < cnt; base += 32) {
-                    const int i = base + lane;
+            if (!rejected) {
+                // -- nearest node of every lane's sample: one pass per tree, nodes
+                // staged 32 at a time in shared memory and read by all lanes
+                float best = FLT_MAX;
+                int bi = 0;
+                for (int tree = 0; tree < 2; tree++) {
+                    if (!__any_sync(FULL, valid && t == tree)) continue;
+                    const int cnt = min(tree == 0 ? f0 : f1, P.cap);
+                    const float *nd = nodes_s + (size_t)tree * D * P.cap;
+                    for (int base = 0; base < cnt; base += 32) {
+                        const int i = base + lane;
 #pragma unroll
-                    for (int d = 0; d < D; d++) W.chunk[d][lane] = i < cnt ? __ldcg(nd + (size_t)d * P.cap + i) : __int_as_float(0x7FFFFFFF);
-                    __syncwarp();
-                    if (valid && t == tree) {
-                        const int m = min(32, cnt - base);
-                        for (int n = 0; n < m; n++) {
-                            float a = 0.0f;
+                        for (int d = 0; d < D; d++)
+                            W.chunk[d][lane] = i < cnt ? __ldcg(nd + (size_t)d * P.cap + i) : __int_as_float(0x7FFFFFFF);
+                        __syncwarp();
+                        if (valid && t == tree) {
+                            const int m = min(32, cnt - base);
+                            for (int n = 0; n < m; n++) {
+                                float a = 0.0f;
 #pragma unroll
-                            for (int d = 0; d < D; d++) {
-                                const float x = W.chunk[d][n] - qv[d];
-                                a = fmaf(x, x, a);
-                            }
-                            if (a < best) {
-                                best = a;
-                                bi = base + n;
+                                for (int d = 0; d < D; d++) {
+                                    const float x = W.chunk[d][n] - qv[d];
+                                    a = fmaf(x, x, a);
+                                }
+                                if (a < best) {
+                                    best = a;
+                                    bi = base + n;
+                                }
                             }
                         }
+                        __syncwarp();
                     }
-                    __syncwarp();
+                    nn_visits += (unsigned long long)cnt * __popc(__ballot_sync(FULL, valid && t == tree));
                 }
-                nn_visits += (unsigned long long)cnt * __popc(__ballot_sync(FULL, valid && t == tree));
-            }
-            const float dist = sqrtf(best);
-            bool go = valid;
-            if (go && P.dynamic_domain) go = !(__ldcg(rad_s + (size_t)t * P.cap + bi) < dist);
-            unsigned todo = __ballot_sync(FULL, go);
+                const float dist = sqrtf(best);
+                bool go = valid;
+                if (go && P.dynamic_domain) go = !(__ldcg(rad_s + (size_t)t * P.cap + bi) < dist);
+                unsigned todo = __ballot_sync(FULL, go);
 
-            // -- extend (and connect) each surviving sample, in lane order
-            while (todo) {
-                const int j = __ffs(todo) - 1;
-                todo &= todo - 1;
-                const int tj = __shfl_sync(FULL, t, j);
-                const int ni = __shfl_sync(FULL, bi, j);
-                const int iterj = __shfl_sync(FULL, iter, j);
-                const float distj = __shfl_sync(FULL, dist, j);
+                // -- extend (and connect) each surviving sample, in lane order
+                while (todo) {
+                    const int j = __ffs(todo) - 1;
+                    todo &= todo - 1;
+                    const int tj = __shfl_sync(FULL, t, j);
+                    const int ni = __shfl_sync(FULL, bi, j);
+                    const int iterj = __shfl_sync(FULL, iter, j);
+                    const float distj = __shfl_sync(FULL, dist, j);
 #pragma unroll
-                for (int d = 0; d < D; d++) {
-                    const float v = __shfl_sync(FULL, qv[d], j);
-                    if (lane == d) W.cfg[d] = v;
-                }
-                const int o = 1 - tj;
-                float *nd_t = nodes_s + (size_t)tj * D * P.cap, *nd_o = nodes_s + (size_t)o * D * P.cap;
-                int *pr_t = par_s + (size_t)tj * P.cap;
-                float *rd_t = rad_s + (size_t)tj * P.cap;
-                const float scale = fminf(1.0f, P.range / distj);
-                if (lane < D) {
-                    const float nn = __ldcg(nd_t + (size_t)lane * P.cap + ni);
-                    const float c = fmaf(W.cfg[lane] - nn, scale, nn);
-                    W.nn[lane] = nn;
-                    W.from[lane] = nn;
-                    W.cfg[lane] = c;
-                    W.step[lane] = __fdiv_rn(__fsub_rn(c, nn), fg);
-                }
-                __syncwarp();
-                if (!warp_validate<Gen>(W, P.granularity, P.edge_order, ctx, C->work)) {
-                    if (lane == 0 && P.dynamic_domain) dd_shrink(rd_t + ni, P.dd_alpha, P.dd_radius, P.dd_min_radius);
-                    continue;
-                }
-                int idx = -1;
-                if (lane == 0) {
-                    idx = atomicAdd(&S->free_index[tj], 1);
-                    if (idx >= P.max_samples || idx >= P.cap) {
-                        finish_attempt(P, S, q, idx >= P.max_samples ? 0 : PRRTC_ENOMEM);
-                        idx = -1;
-                    } else {
-                        pr_t[idx] = ni;
-                        if (P.dynamic_domain) {
-                            rd_t[idx] = FLT_MAX;
-                            dd_grow(rd_t + ni, P.dd_alpha);
-                        }
+                    for (int d = 0; d < D; d++) {
+                        const float v = __shfl_sync(FULL, qv[d], j);
+                        if (lane == d) W.cfg[d] = v;
                     }
-                }
-                idx = __shfl_sync(FULL, idx, 0);
-                if (idx < 0) break;
-                if (lane < D) nd_t[(size_t)lane * P.cap + idx] = W.cfg[lane];
-                __threadfence();
-                __syncwarp();
-                // connect toward the other tree (pRRTC.cu:478-551)
-                float cq[D];
-#pragma unroll
-                for (int d = 0; d < D; d++) cq[d] = W.cfg[d];
-                float dsq;
-                int oi;
-                const int cnt_o = vload(&S->free_index[o]);
-                warp_nn<D>(nd_o, P.cap, cnt_o, cq, dsq, oi);
-                nn_visits += (unsigned long long)min(cnt_o, P.cap);
-                const unsigned n_ext = (unsigned)ceilf(sqrtf(dsq) / P.range);
-                if (lane < D) W.vec[lane] = (__ldcg(nd_o + (size_t)lane * P.cap + oi) - W.cfg[lane]) / (float)n_ext;
-                __syncwarp();
-                unsigned i_ext = 0;
-                int parent = idx;
-                while (i_ext < n_ext) {
+                    const int o = 1 - tj;
+                    float *nd_t = nodes_s + (size_t)tj * D * P.cap, *nd_o = nodes_s + (size_t)o * D * P.cap;
+                    int *pr_t = par_s + (size_t)tj * P.cap;
+                    float *rd_t = rad_s + (size_t)tj * P.cap;
+                    const float scale = fminf(1.0f, P.range / distj);
                     if (lane < D) {
-                        const float a = W.cfg[lane];
-                        const float b = a + W.vec[lane];
-                        W.next[lane] = b;
-                        W.from[lane] = a;
-                        W.step[lane] = __fdiv_rn(__fsub_rn(b, a), fg);
+                        const float nn = __ldcg(nd_t + (size_t)lane * P.cap + ni);
+                        const float c = fmaf(W.cfg[lane] - nn, scale, nn);
+                        W.nn[lane] = nn;
+                        W.from[lane] = nn;
+                        W.cfg[lane] = c;
+                        W.step[lane] = __fdiv_rn(__fsub_rn(c, nn), fg);
                     }
                     __syncwarp();
-                    if (!warp_validate<Gen>(W, P.granularity, P.edge_order, ctx, C->work)) break;
-                    int idx2 = -1;
+                    if (!warp_validate<Gen>(W, P.granularity, P.edge_order, ctx, C->work)) {
+                        if (lane == 0 && P.dynamic_domain)
+                            dd_shrink(rd_t + ni, P.dd_alpha, P.dd_radius, P.dd_min_radius);
+                        continue;
+                    }
+                    int idx = -1;
                     if (lane == 0) {
-                        idx2 = atomicAdd(&S->free_index[tj], 1);
-                        if (idx2 >= P.max_samples || idx2 >= P.cap) {
-                            finish_attempt(P, S, q, idx2 >= P.max_samples ? 0 : PRRTC_ENOMEM);
-                            idx2 = -1;
+                        idx = atomicAdd(&S->free_index[tj], 1);
+                        if (idx >= P.max_samples || idx >= P.cap) {
+                            finish_attempt(P, S, q, idx >= P.max_samples ? 0 : PRRTC_ENOMEM);
+                            idx = -1;
                         } else {
-                            pr_t[idx2] = parent;
-                            rd_t[idx2] = FLT_MAX;
+                            pr_t[idx] = ni;
+                            if (P.dynamic_domain) {
+                                rd_t[idx] = FLT_MAX;
+                                dd_grow(rd_t + ni, P.dd_alpha);
+                            }
                         }
                     }
-                    idx2 = __shfl_sync(FULL, idx2, 0);
-                    if (idx2 < 0) {
-                        parent = -1;
-                        break;
-                    }
-                    if (lane < D) {
-                        W.cfg[lane] = W.next[lane];
-                        nd_t[(size_t)lane * P.cap + idx2] = W.next[lane];
-                    }
+                    idx = __shfl_sync(FULL, idx, 0);
+                    if (idx < 0) break;
+                    if (lane < D) nd_t[(size_t)lane * P.cap + idx] = W.cfg[lane];
                     __threadfence();
                     __syncwarp();
-                    parent = idx2;
-                    i_ext++;
-                }
-                if (i_ext == n_ext && parent >= 0 && lane == 0) {
-                    // connected: end the attempt, then the first attempt to
-                    // win the query traces the path
-                    if (atomicCAS(&S->state, SLOT_RUNNING, SLOT_DONE) == SLOT_RUNNING) {
-                        atomicSub(&P.qstate[q].live, 1);
-                        if (atomicCAS(&P.qstate[q].state, 1, 2) == 1) {
-                            __threadfence();
-                            batch_trace<D>(P, S, slot, q, tj, parent, oi, iterj);
+                    // connect toward the other tree (pRRTC.cu:478-551)
+                    float cq[D];
+#pragma unroll
+                    for (int d = 0; d < D; d++) cq[d] = W.cfg[d];
+                    float dsq;
+                    int oi;
+                    const int cnt_o = vload(&S->free_index[o]);
+                    warp_nn<D>(nd_o, P.cap, cnt_o, cq, dsq, oi);
+                    nn_visits += (unsigned long long)min(cnt_o, P.cap);
+                    const unsigned n_ext = (unsigned)ceilf(sqrtf(dsq) / P.range);
+                    if (lane < D) W.vec[lane] = (__ldcg(nd_o + (size_t)lane * P.cap + oi) - W.cfg[lane]) / (float)n_ext;
+                    __syncwarp();
+                    unsigned i_ext = 0;
+                    int parent = idx;
+                    while (i_ext < n_ext) {
+                        if (lane < D) {
+                            const float a = W.cfg[lane];
+                            const float b = a + W.vec[lane];
+                            W.next[lane] = b;
+                            W.from[lane] = a;
+                            W.step[lane] = __fdiv_rn(__fsub_rn(b, a), fg);
+                        }
+                        __syncwarp();
+                        if (!warp_validate<Gen>(W, P.granularity, P.edge_order, ctx, C->work)) break;
+                        int idx2 = -1;
+                        if (lane == 0) {
+                            idx2 = atomicAdd(&S->free_index[tj], 1);
+                            if (idx2 >= P.max_samples || idx2 >= P.cap) {
+                                finish_attempt(P, S, q, idx2 >= P.max_samples ? 0 : PRRTC_ENOMEM);
+                                idx2 = -1;
+                            } else {
+                                pr_t[idx2] = parent;
+                                rd_t[idx2] = FLT_MAX;
+                            }
+                        }
+                        idx2 = __shfl_sync(FULL, idx2, 0);
+                        if (idx2 < 0) {
+                            parent = -1;
+                            break;
+                        }
+                        if (lane < D) {
+                            W.cfg[lane] = W.next[lane];
+                            nd_t[(size_t)lane * P.cap + idx2] = W.next[lane];
+                        }
+                        __threadfence();
+                        __syncwarp();
+                        parent = idx2;
+                        i_ext++;
+                    }
+                    if (i_ext == n_ext && parent >= 0 && lane == 0) {
+                        // connected: end the attempt, then the first attempt to
+                        // win the query traces the path
+                        if (atomicCAS(&S->state, SLOT_RUNNING, SLOT_DONE) == SLOT_RUNNING) {
+                            atomicSub(&P.qstate[q].live, 1);
+                            if (atomicCAS(&P.qstate[q].state, 1, 2) == 1) {
+                                __threadfence();
+                                batch_trace<D>(P, S, slot, q, tj, parent, oi, iterj);
+                            }
                         }
                     }
+                    __syncwarp();
+                    // stop once the attempt has ended (solved here, or elsewhere)
+                    int ended = 0;
+                    if (lane == 0) ended = vload(&S->state) != SLOT_RUNNING;
+                    if (__shfl_sync(FULL, ended, 0)) break;
                 }
-                __syncwarp();
-                // stop once the attempt has ended (solved here, or elsewhere)
-                int ended = 0;
-                if (lane == 0) ended = vload(&S->state) != SLOT_RUNNING;
-                if (__shfl_sync(FULL, ended, 0)) break;
             }
         }
-        // ---- leave an ended slot
-        int st = 0;
-        if (lane == 0) st = vload(&S->state);
-        st = __shfl_sync(FULL, st, 0);
-        if (st != SLOT_RUNNING) {
-            if (!batch_leave<D>(P, slot, true)) slot = -1;
-        }
+        // an attempt that ended in this round is left at the next round's start
     }
 }
 

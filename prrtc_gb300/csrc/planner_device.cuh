@@ -218,18 +218,26 @@ __device__ __forceinline__ void warp_nn(const float *__restrict__ nodes, int cap
 // because 2^k < M * b <= 2^k + b <= 2^k + 2^(k-32) (Granlund and
 // Montgomery, "Division by invariant integers using multiplication", 1994).
 // magic[b] holds M * 2^(64-k), so q is the high word of one 64-bit product.
-// The sampler's digit loops divide by the Halton bases this way; a rejected
-// sample of a dynamic-domain query is almost nothing but those loops.
+// The sampler's digit loops divide by the Halton bases; a rejected sample of
+// a dynamic-domain query is almost nothing but those loops.  They use the
+// 31-bit form: for i < 2^31, q = floor(i * m / 2^(31 + l)) with
+// l = ceil(log2 b) and m = ceil(2^(31 + l) / b) < 2^32, exact because
+// 0 <= m * b - 2^(31 + l) < b <= 2^l (the same theorem with N = 31), so q is
+// one 32-bit multiply-high and a shift by l - 1.
 struct DivTable {
     unsigned long long magic[65];
+    unsigned m31[65];
+    unsigned s31[65];
     float inv[65];   // 1 / b, correctly rounded
-    constexpr DivTable() : magic(), inv()
+    constexpr DivTable() : magic(), m31(), s31(), inv()
     {
         for (unsigned b = 2; b <= 64; b++) {
             unsigned ell = 0;
             while ((1u << ell) < b) ell++;
             const unsigned k = 32 + ell;
             magic[b] = ((1ull << k) / b + 1) << (64 - k);
+            m31[b] = (unsigned)(((1ull << (31 + ell)) + b - 1) / b);
+            s31[b] = ell - 1;
             inv[b] = 1.0f / (float)b;
         }
     }
@@ -239,6 +247,12 @@ __constant__ const DivTable kDivTable = DivTable();
 __device__ __forceinline__ unsigned div_by(unsigned i, unsigned long long magic)
 {
     return (unsigned)__umul64hi((unsigned long long)i, magic);
+}
+
+// floor(i / b) for i < 2^31 (m = m31[b], s = s31[b])
+__device__ __forceinline__ unsigned div31(unsigned i, unsigned m, unsigned s)
+{
+    return __umulhi(i, m) >> s;
 }
 
 // Radical inverse of index i in integer base b, float32 (the closed form of
@@ -276,43 +290,76 @@ __device__ __forceinline__ float scrambled_radical_inverse(unsigned i, unsigned 
     return r;
 }
 
-// Radical inverses of one index in N bases at once (h[d] in base b[d], each
-// digit multiplied by a[d] mod b[d] when SCRAMBLE).  The digit chains of the N
-// dimensions advance together, one digit of every dimension per trip, for as
-// many trips as the smallest base needs: N independent dependency chains
-// instead of N loops in a row, and the same trip count on every lane.  A
-// dimension whose index is exhausted adds fmaf(f, 0, h) = h, so every h[d] is
-// bit-identical to radical_inverse / scrambled_radical_inverse.
+// Radical inverses of one index iter < 2^31 in N bases at once (h[d] in base
+// b[d], each digit multiplied by a[d] mod b[d] when SCRAMBLE).  The digit
+// chains of the N dimensions advance together, one digit of every dimension
+// per trip, for as many trips as the smallest base needs: N independent
+// dependency chains instead of N loops in a row, and the same trip count on
+// every lane.  A dimension whose index is exhausted adds fmaf(f, 0, h) = h, so
+// every h[d] is bit-identical to radical_inverse / scrambled_radical_inverse.
+//
+// The state can stop between trips: after any trip, h[d] holds the digits so
+// far and the digits still to come add less than f[d] * b[d] (each at most
+// b - 1 times a weight f, f / b, ...), nothing at all once idx[d] is 0.
+template <int N, bool SCRAMBLE>
+struct RadicalDigits {
+    unsigned idx[N], m[N], s[N], b[N], a[N];
+    float f[N], inv[N], h[N];
+    unsigned rem, mmin, smin;
+
+    __device__ __forceinline__ RadicalDigits(unsigned iter, const unsigned (&bs)[N], const unsigned (&as)[N])
+    {
+        unsigned bmin = bs[0];
+#pragma unroll
+        for (int d = 0; d < N; d++) {
+            b[d] = bs[d];
+            a[d] = as[d];
+            idx[d] = iter;
+            m[d] = kDivTable.m31[b[d]];
+            s[d] = kDivTable.s31[b[d]];
+            inv[d] = kDivTable.inv[b[d]];
+            f[d] = inv[d];
+            h[d] = 0.0f;
+            bmin = min(bmin, b[d]);
+        }
+        mmin = kDivTable.m31[bmin];
+        smin = kDivTable.s31[bmin];
+        rem = iter;
+    }
+    __device__ __forceinline__ void trip()
+    {
+#pragma unroll
+        for (int d = 0; d < N; d++) {
+            const unsigned q = div31(idx[d], m[d], s[d]);
+            unsigned dig = idx[d] - q * b[d];
+            if (SCRAMBLE) {
+                const unsigned t = a[d] * dig;   // < 64 * 64
+                dig = t - div31(t, m[d], s[d]) * b[d];
+            }
+            h[d] = fmaf(f[d], (float)dig, h[d]);
+            idx[d] = q;
+            f[d] *= inv[d];
+        }
+        rem = div31(rem, mmin, smin);
+    }
+    __device__ __forceinline__ void run(int trips)
+    {
+        for (int k = 0; k < trips && rem > 0; k++) trip();
+    }
+    __device__ __forceinline__ void finish()
+    {
+        while (rem > 0) trip();
+    }
+};
+
 template <int N, bool SCRAMBLE>
 __device__ __forceinline__ void radical_inverses(unsigned iter, const unsigned (&b)[N], const unsigned (&a)[N],
                                                  float (&h)[N])
 {
-    unsigned idx[N];
-    float f[N];
-    unsigned bmin = b[0];
+    RadicalDigits<N, SCRAMBLE> r(iter, b, a);
+    r.finish();
 #pragma unroll
-    for (int d = 0; d < N; d++) {
-        idx[d] = iter;
-        f[d] = kDivTable.inv[b[d]];
-        h[d] = 0.0f;
-        bmin = min(bmin, b[d]);
-    }
-    const unsigned long long mmin = kDivTable.magic[bmin];
-    for (unsigned rem = iter; rem > 0; rem = div_by(rem, mmin)) {
-#pragma unroll
-        for (int d = 0; d < N; d++) {
-            const unsigned long long mg = kDivTable.magic[b[d]];
-            const unsigned q = div_by(idx[d], mg);
-            unsigned dig = idx[d] - q * b[d];
-            if (SCRAMBLE) {
-                const unsigned t = a[d] * dig;
-                dig = t - div_by(t, mg) * b[d];
-            }
-            h[d] = fmaf(f[d], (float)dig, h[d]);
-            idx[d] = q;
-            f[d] *= kDivTable.inv[b[d]];
-        }
-    }
+    for (int d = 0; d < N; d++) h[d] = r.h[d];
 }
 
 __device__ __forceinline__ unsigned hash32(unsigned x)

@@ -117,6 +117,10 @@ struct BatchCounters {
     unsigned long long nn_nodes;     // tree nodes visited by nearest-neighbour scans
 };
 
+// cap on a batch query's samples: 2^31 - 2^24, so that tickets taken past it
+// by every resident warp (32 each) still fit an int
+constexpr long long kMaxSamplesDrawn = 0x7f000000LL;
+
 struct BatchParams {
     int max_samples, max_iters, lanes, granularity;
     float range;
