@@ -253,6 +253,9 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     P.max_iters = S.max_iters;
     P.lanes = b->lanes;
     P.granularity = S.granularity;
+    int max_records = 0;
+    for (int i = 0; i < n; i++) max_records = std::max(max_records, descs[i].env_n.records());
+    P.env_records = std::min(max_records, kWarpEnvRecords);
     P.range = S.range;
     P.balance = S.balance;
     P.tree_ratio = S.tree_ratio;
@@ -290,7 +293,7 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     P.halton_bases = c->bases;
     prrtc_robot_limits(robot, P.scale, P.offset);
     // launch shape
-    const int occ = ops->batch_occupancy(b->wpb);
+    const int occ = ops->batch_occupancy(b->wpb, P.env_records);
     int per_sm = settings->blocks_per_sm > 0 ? std::min(settings->blocks_per_sm, std::max(occ, 1)) : std::max(occ, 1);
     b->blocks = c->sms * per_sm;
     b->stats.blocks = b->blocks;

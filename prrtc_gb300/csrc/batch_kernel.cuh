@@ -29,19 +29,24 @@ namespace prrtc {
 // Obstacle records a warp keeps in shared memory for the query it works on
 // (4 KB: Panda and Fetch scenes and most Baxter ones); larger scenes are
 // read from global memory through L1.
-constexpr int kWarpEnvRecords = 256;
-
-struct WarpScratch {
-    float4 env[kWarpEnvRecords];
-    float from[16], step[16], cfg[16], nn[16], vec[16], next[16];
-    float chunk[16][33];   // 32 tree nodes staged for the round's nearest-neighbour pass (+1: bank skew)
-    float dom[7][33];      // early rejection: the first coordinates of a small tree's nodes,
-    float rad2[32];        // their squared widened domain radii
+// Per-warp shared scratch of the batched planner, followed in shared memory
+// by the warp's staged obstacle records (BatchParams::env_records of them).
+template <int D>
+struct alignas(16) WarpScratch {
+    float from[D], step[D], cfg[D], nn[D], vec[D], next[D];
+    float chunk[D][33];    // 32 tree nodes staged for the round's nearest-neighbour pass (+1: bank skew);
+                           // early rejection stages its nodes' first coordinates here before that pass
+    float rad2[32];        // early rejection: the staged nodes' squared widened domain radii
     float box_lo[8], box_hi[8];   // and the box around all their domains
     unsigned hsh[16];      // scrambled sampler: the hash of (query, attempt, dimension)
     int bad;
-    int pad_[3];
 };
+
+template <int D>
+__host__ __device__ constexpr size_t warp_scratch_bytes(int env_records)
+{
+    return sizeof(WarpScratch<D>) + (size_t)env_records * sizeof(float4);
+}
 
 // Exact early rejection of dynamic-domain samples.  When every lane of a
 // round samples the same tree and it has at most 32 nodes (a trapped tree
@@ -60,12 +65,16 @@ constexpr int kEarlyTrips = 4;
 constexpr float kEarlyRel = 1.0f / 1024.0f, kEarlyAbs = 1.0f / 65536.0f;
 constexpr int kEarlyBox = 8;
 
+// warps an attempt admits: kJoinBase plus one per kJoinTickets samples drawn
+// (so the cap doubles about every two rounds), up to max_workers
+constexpr int kJoinBase = 4, kJoinTickets = 64;
+
 // whole warp: stage the first G coordinates and the widened radii of the
 // tree's first cnt (<= 32) nodes and, above kEarlyBox nodes, the box around
 // their domains.  A node with a NaN coordinate or radius (an insertion in
 // flight) makes the box unbounded in that dimension.
-template <int G>
-__device__ __forceinline__ void stage_domains(WarpScratch &W, const float *nd, const float *rd, int cap, int cnt)
+template <int G, class WS>
+__device__ __forceinline__ void stage_domains(WS &W, const float *nd, const float *rd, int cap, int cnt)
 {
     const int lane = lane_id();
     const bool have = lane < cnt;
@@ -75,7 +84,7 @@ __device__ __forceinline__ void stage_domains(WarpScratch &W, const float *nd, c
 #pragma unroll
     for (int j = 0; j < G; j++) {
         const float c = have ? __ldcg(nd + (size_t)j * cap + lane) : 0.0f;
-        W.dom[j][lane] = c;
+        W.chunk[j][lane] = c;
         if (cnt <= kEarlyBox) continue;
         float lo = c - m, hi = c + m;
         if (!have) {
@@ -104,9 +113,9 @@ __device__ __forceinline__ void stage_domains(WarpScratch &W, const float *nd, c
 // the remaining fmaf steps; the scrambled sampler's rotation keeps an
 // interval unless it wraps past 1.  Coordinates are fmaf(v, scale, offset),
 // monotone in v.  A NaN anywhere answers yes.
-template <int G, bool SCRAMBLE>
+template <int G, bool SCRAMBLE, class WS>
 __device__ __forceinline__ bool early_near(const RadicalDigits<G, SCRAMBLE> &r, const unsigned (&hsh)[G],
-                                           const BatchParams &P, const WarpScratch &W, int cnt)
+                                           const BatchParams &P, const WS &W, int cnt)
 {
     float lo[G], hi[G];
     bool in_box = true;
@@ -137,7 +146,7 @@ __device__ __forceinline__ bool early_near(const RadicalDigits<G, SCRAMBLE> &r, 
             float acc = 0.0f;
 #pragma unroll
             for (int j = 0; j < G; j++) {
-                const float c = W.dom[j][n];
+                const float c = W.chunk[j][n];
                 const float g = fmaxf(fmaxf(c - hi[j], lo[j] - c), 0.0f);
                 acc = fmaf(g, g, acc);
             }
@@ -151,14 +160,14 @@ __device__ __forceinline__ bool early_near(const RadicalDigits<G, SCRAMBLE> &r, 
 // qv.  With `early` (first group only), returns true when the early test
 // rejected every lane's sample; qv is then incomplete.
 template <int D, int G, bool SCRAMBLE>
-__device__ __forceinline__ bool sample_group(const BatchParams &P, const WarpScratch &W, unsigned iter, int d0,
+__device__ __forceinline__ bool sample_group(const BatchParams &P, const WarpScratch<D> &W, unsigned iter, int d0,
                                              const unsigned (&bs)[G], const unsigned (&as)[G],
                                              const unsigned (&hsh)[G], bool early, int cnt, bool valid, float (&qv)[D])
 {
     RadicalDigits<G, SCRAMBLE> r(iter, bs, as);
     if (early) {
         r.run(kEarlyTrips);
-        const bool near = valid && early_near<G, SCRAMBLE>(r, hsh, P, W, cnt);
+        const bool near = valid && early_near<G, SCRAMBLE, WarpScratch<D>>(r, hsh, P, W, cnt);
         if (!__any_sync(0xffffffffu, near)) return true;
     }
     r.finish();
@@ -183,7 +192,7 @@ __device__ __forceinline__ bool sample_group(const BatchParams &P, const WarpScr
 // lane * R + r + 1, so the first round already samples the whole edge at
 // stride R.  Adds the work done to work[0] (FLOPs) and work[1] (points).
 template <class Gen>
-__device__ __forceinline__ bool warp_validate(const WarpScratch &W, int g, int interleave, CheckCtx &ctx,
+__device__ __forceinline__ bool warp_validate(const WarpScratch<Gen::kDof> &W, int g, int interleave, CheckCtx &ctx,
                                               unsigned long long *work)
 {
     constexpr int D = Gen::kDof;
@@ -497,7 +506,9 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
     constexpr int D = Gen::kDof;
     constexpr unsigned FULL = 0xffffffffu;
     extern __shared__ float4 s_raw[];
-    WarpScratch &W = reinterpret_cast<WarpScratch *>(s_raw)[threadIdx.x >> 5];
+    char *const warp_smem = reinterpret_cast<char *>(s_raw) + (threadIdx.x >> 5) * warp_scratch_bytes<D>(P.env_records);
+    WarpScratch<D> &W = *reinterpret_cast<WarpScratch<D> *>(warp_smem);
+    float4 *const W_env = reinterpret_cast<float4 *>(warp_smem + sizeof(WarpScratch<D>));
     const int lane = lane_id();
     BatchCounters *C = P.ctr;
     const float fg = (float)P.granularity;
@@ -511,7 +522,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
     int cq = 0, catt = 0;   // the slot's query and attempt, read when this warp takes the slot
     bool fresh = true;
     unsigned idle = 0;
-    const float4 *staged = nullptr;   // the global records now in W.env
+    const float4 *staged = nullptr;   // the global records now in W_env
     unsigned long long nn_visits = 0;   // flushed once per warp (a shared counter would serialise)
     auto flush = [&]() {
         if (lane == 0 && nn_visits) atomicAdd(&C->nn_nodes, nn_visits);
@@ -559,7 +570,12 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                     } else if (st == SLOT_FREE && free_slot < 0 && P.max_attempts > 1) {
                         if (atomicCAS(&S->state, SLOT_FREE, SLOT_BUSY) == SLOT_FREE) free_slot = s;
                     } else if (st == SLOT_RUNNING) {
-                        if (vload(&S->workers) >= P.max_workers) continue;
+                        // a young attempt takes few warps: warps that join in its
+                        // first round all see two one-node trees and send half their
+                        // samples to the free one, whose connect steps would then
+                        // fill the arena at once
+                        const int ramp = kJoinBase + vload(&S->ticket) / kJoinTickets;
+                        if (vload(&S->workers) >= min(P.max_workers, ramp)) continue;
                         joinable = 1;
                         atomicAdd(&S->workers, 1);
                         if (vload(&S->state) == SLOT_RUNNING)
@@ -660,14 +676,14 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
         const int q = cq, attempt = catt;
         const BatchQueryDesc Qd = P.queries[q];
         const float4 *envp = Qd.env;
-        if (Qd.env_n.records() <= kWarpEnvRecords) {
+        if (Qd.env_n.records() <= P.env_records) {
             if (staged != Qd.env) {   // the records are read-only for the whole launch
                 __syncwarp();
-                for (int i = lane; i < Qd.env_n.records(); i += 32) W.env[i] = __ldg(Qd.env + i);
+                for (int i = lane; i < Qd.env_n.records(); i += 32) W_env[i] = __ldg(Qd.env + i);
                 __syncwarp();
                 staged = Qd.env;
             }
-            envp = W.env;
+            envp = W_env;
         }
         CheckCtx ctx{{envp, Qd.env_n}, P.pad, &W.bad};
         float *nodes_s = P.nodes + (size_t)slot * 2 * D * P.cap;

@@ -120,9 +120,13 @@ struct BatchCounters {
 // cap on a batch query's samples: 2^31 - 2^24, so that tickets taken past it
 // by every resident warp (32 each) still fit an int
 constexpr long long kMaxSamplesDrawn = 0x7f000000LL;
+// obstacle records a planner warp stages in shared memory (larger
+// environments are read from global memory)
+constexpr int kWarpEnvRecords = 256;
 
 struct BatchParams {
     int max_samples, max_iters, lanes, granularity;
+    int env_records;     // records each warp can stage: the batch's largest environment, <= kWarpEnvRecords
     float range;
     int balance;
     float tree_ratio;
@@ -203,7 +207,7 @@ struct RobotOps {
     cudaError_t (*fk_spheres)(const float *q, int64_t n, float *out, int sms, cudaStream_t);
     cudaError_t (*solve_plain)(const PlainParams &, int threads, cudaStream_t);
     cudaError_t (*solve_batch)(const BatchParams &, int blocks, int warps_per_block, cudaStream_t);
-    int (*batch_occupancy)(int warps_per_block);   // resident blocks per SM
+    int (*batch_occupancy)(int warps_per_block, int env_records);   // resident blocks per SM
     cudaError_t (*smooth_paths)(const ClrLaunch &, size_t env_bytes, cudaStream_t);
     cudaError_t (*goal_flags)(const LaunchEnv &, const GoalQuery &, uint8_t *flags, cudaStream_t);
 };

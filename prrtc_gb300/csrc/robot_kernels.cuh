@@ -403,15 +403,15 @@ struct RobotKernels {
     }
     static cudaError_t solve_batch(const BatchParams &P, int blocks, int wpb, cudaStream_t st)
     {
-        const size_t smem = sizeof(WarpScratch) * wpb;
+        const size_t smem = warp_scratch_bytes<Gen::kDof>(P.env_records) * wpb;
         k_rrtc_batch<Gen><<<blocks, 32 * wpb, smem, st>>>(P);
         return cudaGetLastError();
     }
-    static int batch_occupancy(int wpb)
+    static int batch_occupancy(int wpb, int env_records)
     {
         int n = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_rrtc_batch<Gen>, 32 * wpb, sizeof(WarpScratch) * wpb) !=
-            cudaSuccess) {
+        const size_t smem = warp_scratch_bytes<Gen::kDof>(env_records) * wpb;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_rrtc_batch<Gen>, 32 * wpb, smem) != cudaSuccess) {
             cudaGetLastError();
             return 0;
         }
