@@ -8,8 +8,11 @@ JSON line (the contract this repository's driver reads):
   value      solved queries/s of the batched persistent kernel, inputs resident
              in HBM, timed with CUDA events on the launching stream, L2
              flushed between steps
-  e2e        the same through prrtc_solve_batch with host buffers (upload,
-             solve, download inside the timed region)
+  e2e        the same through the C ABI, prrtc_solve_batch, on host buffers
+             (the prrtc_query array a C or C++ caller passes; upload, solve
+             and download of results and paths inside the timed call);
+             e2e_python: the same through the Python wrapper, marshalling
+             and unpacking included
   plain      the drop-in single-query form (prrtc_solve) on a sample of the
              same queries, one at a time
   roofline   the planner kernel's algorithmic FP32 FLOPs (counted in-kernel:
@@ -54,6 +57,7 @@ MARGIN = 1e-5   # planning margin (m): every returned path clears contact by 10 
 GPU_BUDGET_NS = int(30e9)   # per batch launch; unsolved queries past it count as failures
 CPU_BUDGET_S = 20.0         # per query in the CPU restatement
 PLAIN_BUDGET_S = 30.0       # total for the plain-form comparison
+PLAIN_QUERIES = 128         # the plain form's sample of the first step's queries
 
 
 def log(*a):
@@ -247,16 +251,26 @@ def ours(args, rank, world):
     value = solved / t_dev
     lat = [r.kernel_ns / 1e6 for r in results if r.solved]
 
-    # ---- e2e through the C ABI with host buffers (same streamed job)
+    # ---- e2e through the C ABI with host buffers (same streamed job): the
+    # prrtc_query array points at host start, goal and obstacle arrays, as a C
+    # or C++ caller's would; the timed call uploads them, runs the batch and
+    # copies results and paths back into host buffers
     host_q = [(q.env, q.start, q.goal) for q in qs]
     bs_host = BatchSettings(plan, max_active=n, **common)
     ctx.solve_batch(robot, host_q[:64], BatchSettings(plan, **common))
     torch.cuda.synchronize()
+    prep = ctx.prepare_batch(robot, host_q, path_capacity=2048)
     t0 = time.perf_counter()
-    res_e2e = ctx.solve_batch(robot, host_q, bs_host, path_capacity=2048)
+    ctx.solve_prepared(prep, bs_host)
     e2e_t = time.perf_counter() - t0
+    res_e2e = prep.results()
     e2e_solved = sum(r.solved for r in res_e2e)
     d2h = sum(len(r.path) * r.path.shape[1] * 4 for r in res_e2e) + 64 * len(res_e2e)
+    # the same job through the Python wrapper (marshalling and unpacking timed)
+    t0 = time.perf_counter()
+    res_py = ctx.solve_batch(robot, host_q, bs_host, path_capacity=2048)
+    e2e_py_t = time.perf_counter() - t0
+    e2e_py_solved = sum(r.solved for r in res_py)
 
     if rank != 0:
         return
@@ -270,7 +284,7 @@ def ours(args, rank, world):
     plain_t, plain_solved, plain_ms = 0.0, 0, []
     ctx.set_planning_margin(MARGIN)
     ctx.set_time_budget(int(GPU_BUDGET_NS))
-    for q, e in zip(first, envs[:n]):
+    for q, e in zip(first[:PLAIN_QUERIES], envs[:PLAIN_QUERIES]):
         r = ctx.solve(robot, q.start, q.goal, e, plan)
         plain_t += r.wall_ns * 1e-9
         plain_solved += r.solved
@@ -327,6 +341,8 @@ def ours(args, rank, world):
                   "solved": plain_solved, "batched_over_plain": value / plain_qps},
         "e2e": {"value": e2e_solved / e2e_t, "unit": "queries/s", "h2d_bytes_per_step": h2d_bytes(qs) // args.steps,
                 "d2h_bytes_per_step": d2h // args.steps},
+        "e2e_python": {"value": e2e_py_solved / e2e_py_t, "unit": "queries/s",
+                       "note": "Context.solve_batch: the Python wrapper's marshalling and unpacking included"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak,
                      "traffic": (lambda b: b * len(qs) if b else None)(profiled_dram_bytes_per_query(args.workload)),
@@ -464,8 +480,10 @@ def main():
     ap.add_argument("--queries", type=int, default=1024)
     ap.add_argument("--no-clearance", dest="clearance", action="store_false",
                     help="skip the path-smoothing measurement")
-    ap.add_argument("--no-others", dest="others", action="store_false",
-                    help="skip the one-launch runs of the other configurations")
+    ap.add_argument("--others", action="store_true",
+                    help="also run the other configurations (Panda tabletop, Fetch, Baxter) one launch each; "
+                         "they are parity cases, not the benchmark, and Baxter's launches run to a 10 s budget")
+    ap.add_argument("--no-others", dest="others", action="store_false", help=argparse.SUPPRESS)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -391,9 +391,16 @@ class Context:
         return Batch(self, robot, queries, settings if settings is not None else BatchSettings(), path_capacity)
 
     def solve_batch(self, robot, queries, settings: BatchSettings | None = None, path_capacity: int = 4096) -> list:
-        """prrtc_solve_batch: upload, solve and download in one call.  The
-        query, descriptor and result arrays are built as numpy arrays with the
-        C structs' layouts (no per-query ctypes work)."""
+        """prrtc_solve_batch: upload, solve and download in one call."""
+        prep = self.prepare_batch(robot, queries, path_capacity)
+        self.solve_prepared(prep, settings)
+        return prep.results()
+
+    def prepare_batch(self, robot, queries, path_capacity: int = 4096) -> "PreparedBatch":
+        """The host side of prrtc_solve_batch's arguments: the prrtc_query
+        array (pointing at host start, goal and obstacle arrays) and the
+        prrtc_result array with its path buffers, built as numpy arrays with
+        the C structs' layouts (no per-query ctypes work)."""
         rid = robot_id(robot)
         D, n = dof(rid), len(queries)
         trip = [q if isinstance(q, tuple) else (q.env, q.start, q.goal) for q in queries]
@@ -427,15 +434,15 @@ class Context:
         res = np.zeros(n, _RESULT_DT)
         res["path_capacity"] = path_capacity
         res["path"] = paths.ctypes.data + 4 * D * path_capacity * np.arange(n, dtype=np.uint64)
+        return PreparedBatch(rid, qs, res, paths, keep)
+
+    def solve_prepared(self, prep: "PreparedBatch", settings: BatchSettings | None = None) -> None:
+        """The prrtc_solve_batch call itself on prepared host arrays; the
+        answers land in prep.res and prep.paths."""
         s = settings if settings is not None else BatchSettings()
-        self._check(lib().prrtc_solve_batch(self.handle, rid, C.cast(C.c_void_p(qs.ctypes.data), C.POINTER(_Query)), n,
-                                            C.byref(s), C.cast(C.c_void_p(res.ctypes.data), C.POINTER(_Result))))
-        cols = {f: res[f].tolist() for f in ("solved", "path_rows", "start_tree_size", "goal_tree_size", "path_length",
-                                             "iters", "cost", "wall_ns", "kernel_ns", "copy_ns", "status")}
-        return [PlannerResult(bool(cols["solved"][i]), paths[i, :cols["path_rows"][i]].copy(), cols["start_tree_size"][i],
-                              cols["goal_tree_size"][i], cols["path_length"][i], cols["iters"][i], cols["cost"][i],
-                              cols["wall_ns"][i], cols["kernel_ns"][i], cols["copy_ns"][i], cols["status"][i])
-                for i in range(n)]
+        self._check(lib().prrtc_solve_batch(self.handle, prep.rid, C.cast(C.c_void_p(prep.qs.ctypes.data), C.POINTER(_Query)),
+                                            len(prep.qs), C.byref(s),
+                                            C.cast(C.c_void_p(prep.res.ctypes.data), C.POINTER(_Result))))
 
     def solve(self, robot, start, goals, env, settings: Settings | None = None, path_capacity: int = 70000) -> PlannerResult:
         """pRRTC::solve<Robot>(start, goals, env, settings)."""
@@ -456,6 +463,27 @@ class Context:
         return PlannerResult(bool(r.solved), path[:r.path_rows].copy() if r.solved else np.zeros((0, D), np.float32),
                              r.start_tree_size, r.goal_tree_size, r.path_length, r.iters, r.cost, r.wall_ns,
                              r.kernel_ns, r.copy_ns, r.status)
+
+
+@dataclass
+class PreparedBatch:
+    """prrtc_solve_batch's host arguments (Context.prepare_batch): the query
+    and result arrays in the C layouts, the path buffers, and the host arrays
+    they point into."""
+    rid: int
+    qs: np.ndarray
+    res: np.ndarray
+    paths: np.ndarray
+    keep: list
+
+    def results(self) -> list:
+        res, paths = self.res, self.paths
+        cols = {f: res[f].tolist() for f in ("solved", "path_rows", "start_tree_size", "goal_tree_size", "path_length",
+                                             "iters", "cost", "wall_ns", "kernel_ns", "copy_ns", "status")}
+        return [PlannerResult(bool(cols["solved"][i]), paths[i, :cols["path_rows"][i]].copy(), cols["start_tree_size"][i],
+                              cols["goal_tree_size"][i], cols["path_length"][i], cols["iters"][i], cols["cost"][i],
+                              cols["wall_ns"][i], cols["kernel_ns"][i], cols["copy_ns"][i], cols["status"][i])
+                for i in range(len(res))]
 
 
 class Batch:

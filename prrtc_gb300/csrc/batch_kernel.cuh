@@ -65,9 +65,10 @@ constexpr int kEarlyTrips = 4;
 constexpr float kEarlyRel = 1.0f / 1024.0f, kEarlyAbs = 1.0f / 65536.0f;
 constexpr int kEarlyBox = 8;
 
-// warps an attempt admits: kJoinBase plus one per kJoinTickets samples drawn
-// (so the cap doubles about every two rounds), up to max_workers
-constexpr int kJoinBase = 4, kJoinTickets = 64;
+// warps an attempt admits: kJoinBase for its first kJoinYoungNs, then up to
+// max_workers
+constexpr int kJoinBase = 4;
+constexpr unsigned long long kJoinYoungNs = 200000;
 
 // whole warp: stage the first G coordinates and the widened radii of the
 // tree's first cnt (<= 32) nodes and, above kEarlyBox nodes, the box around
@@ -387,6 +388,7 @@ __device__ void batch_admit(const BatchParams &P, int s, int qa, int attempt)
         S->query = qa;
         S->attempt = attempt;
         S->restart = 0;
+        S->t_start = global_ns();
         S->free_index[0] = 1;
         S->free_index[1] = Q.num_goals;
         S->ticket = 0;
@@ -551,6 +553,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
             if (lane == 0) {
                 s0 = atomicAdd((unsigned *)&C->cursor, 1u);
                 const bool pending = vload(&C->admit_next) < P.num_queries;
+                const unsigned long long now = global_ns();
                 for (int tries = 0; tries < P.num_slots; tries++) {
                     const int s = (int)((s0 + (unsigned)tries) % (unsigned)P.num_slots);
                     SlotState *S = &P.slots[s];
@@ -570,12 +573,18 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                     } else if (st == SLOT_FREE && free_slot < 0 && P.max_attempts > 1) {
                         if (atomicCAS(&S->state, SLOT_FREE, SLOT_BUSY) == SLOT_FREE) free_slot = s;
                     } else if (st == SLOT_RUNNING) {
-                        // a young attempt takes few warps: warps that join in its
-                        // first round all see two one-node trees and send half their
-                        // samples to the free one, whose connect steps would then
-                        // fill the arena at once
-                        const int ramp = kJoinBase + vload(&S->ticket) / kJoinTickets;
-                        if (vload(&S->workers) >= min(P.max_workers, ramp)) continue;
+                        const int w = vload(&S->workers);
+                        if (w >= P.max_workers) continue;
+                        // a young attempt takes few warps: idle warps that all join
+                        // it at once (the tail of a stream) see two small trees,
+                        // send half their samples to the free one, and its connect
+                        // steps fill the arena.  It counts as joinable all the same
+                        // (the warp waits for it instead of forcing another attempt).
+                        if (w >= kJoinBase &&
+                            now - *(const volatile unsigned long long *)&S->t_start < kJoinYoungNs) {
+                            joinable = 1;
+                            continue;
+                        }
                         joinable = 1;
                         atomicAdd(&S->workers, 1);
                         if (vload(&S->state) == SLOT_RUNNING)

@@ -78,6 +78,7 @@ struct SlotState {
     int ticket;          // samples drawn so far
     int workers;         // warps registered on the slot
     int restart;         // 1: the warp that recycles the slot restarts the query here
+    unsigned long long t_start;   // device ns when the slot's attempt was admitted
 };
 
 // Per-query state shared by its attempts.
