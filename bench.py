@@ -340,7 +340,8 @@ def ours(args, rank, world):
                   "max_solve_ms": max(plain_ms), "sample": f"{ns_plain} of the first step's {n} queries",
                   "solved": plain_solved, "batched_over_plain": value / plain_qps},
         "e2e": {"value": e2e_solved / e2e_t, "unit": "queries/s", "h2d_bytes_per_step": h2d_bytes(qs) // args.steps,
-                "d2h_bytes_per_step": d2h // args.steps},
+                "d2h_bytes_per_step": d2h // args.steps, "call_ms": e2e_t * 1e3,
+                "create_ms": res_e2e[0].copy_ns / 1e6 if res_e2e else None},
         "e2e_python": {"value": e2e_py_solved / e2e_py_t, "unit": "queries/s",
                        "note": "Context.solve_batch: the Python wrapper's marshalling and unpacking included"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
