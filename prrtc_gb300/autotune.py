@@ -32,7 +32,7 @@ TUNING = Path(__file__).resolve().parent / "tuning.json"
 DEFAULT = {"lanes": 1, "warps_per_block": 2, "edge_order": 0, "sampler": 0, "max_workers_per_attempt": 0,
            "max_attempts": 4}
 SPACE = {"lanes": (1, 2), "warps_per_block": (2, 4), "edge_order": (0, 1), "sampler": (0, 1),
-         "max_workers_per_attempt": (64, 0), "max_attempts": (4,)}
+         "max_workers_per_attempt": (64, 0), "max_attempts": (1, 4)}
 KNOBS = tuple(SPACE)
 
 

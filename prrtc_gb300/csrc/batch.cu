@@ -181,8 +181,9 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     const size_t slot_bytes = (size_t)2 * cap * (D + 2) * sizeof(float);
     const size_t arena_budget = (size_t)32 << 30;
     const int max_attempts = settings->max_attempts > 0 ? settings->max_attempts : 4;
-    int slots = settings->max_active > 0 ? std::min(settings->max_active, n) : n;
-    if (max_attempts > 1) slots += std::max(64, n / 4);   // room for extra attempts in the tail
+    const int active = settings->max_active > 0 ? std::min(settings->max_active, n) : n;
+    int slots = active;
+    if (max_attempts > 1) slots += std::max(64, n / 4);   // room for restarts and extra attempts
     slots = (int)std::max<size_t>(1, std::min<size_t>(slots, arena_budget / slot_bytes));
     b->slots = slots;
     b->path_rows = std::max(4096, n * 512);
@@ -267,6 +268,7 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     P.budget_ns = settings->time_budget_ns;
     P.num_queries = n;
     P.num_slots = slots;
+    P.admit_slots = std::min(active, slots);
     P.cap = cap;
     P.path_pool_rows = b->path_rows;
     P.edge_order = settings->edge_order ? 1 : 0;

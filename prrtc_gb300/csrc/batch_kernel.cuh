@@ -457,7 +457,7 @@ __device__ bool batch_leave(const BatchParams &P, int s, bool allow_admit)
                 finish_query_unsolved(P, S, q, 0);
             }
         }
-        if (qa < 0 && vload(&P.ctr->admit_next) < P.num_queries) {
+        if (qa < 0 && s < P.admit_slots && vload(&P.ctr->admit_next) < P.num_queries) {
             qa = atomicAdd(&P.ctr->admit_next, 1);
             if (qa >= P.num_queries) {
                 qa = -1;
@@ -548,7 +548,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
         // ---- find work: a pending query, else a running attempt with room for
         // another warp; in the tail, free slots become extra attempts
         if (slot < 0) {
-            int found = -1, admit = -1, rec = -1, free_slot = -1, joinable = 0;
+            int found = -1, admit = -1, rec = -1, free_slot = -1, free_cand = -1, joinable = 0;
             unsigned s0 = 0;
             if (lane == 0) {
                 s0 = atomicAdd((unsigned *)&C->cursor, 1u);
@@ -558,7 +558,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                     const int s = (int)((s0 + (unsigned)tries) % (unsigned)P.num_slots);
                     SlotState *S = &P.slots[s];
                     const int st = vload(&S->state);
-                    if (st == SLOT_FREE && pending) {
+                    if (st == SLOT_FREE && pending && s < P.admit_slots) {
                         if (atomicCAS(&S->state, SLOT_FREE, SLOT_BUSY) != SLOT_FREE) continue;
                         int qa = atomicAdd(&C->admit_next, 1);
                         if (qa < P.num_queries) {
@@ -570,8 +570,8 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                             break;
                         }
                         atomicExch(&S->state, SLOT_FREE);
-                    } else if (st == SLOT_FREE && free_slot < 0 && P.max_attempts > 1) {
-                        if (atomicCAS(&S->state, SLOT_FREE, SLOT_BUSY) == SLOT_FREE) free_slot = s;
+                    } else if (st == SLOT_FREE && free_cand < 0 && P.max_attempts > 1 && !pending) {
+                        free_cand = s;   // claimed below, only if there is nothing to join
                     } else if (st == SLOT_RUNNING) {
                         const int w = vload(&S->workers);
                         if (w >= P.max_workers) continue;
@@ -594,10 +594,9 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                         break;
                     }
                 }
-                if (free_slot >= 0 && (found >= 0 || rec >= 0)) {
-                    atomicExch(&P.slots[free_slot].state, SLOT_FREE);
-                    free_slot = -1;
-                }
+                if (free_cand >= 0 && found < 0 && rec < 0 &&
+                    atomicCAS(&P.slots[free_cand].state, SLOT_FREE, SLOT_BUSY) == SLOT_FREE)
+                    free_slot = free_cand;
             }
             found = __shfl_sync(FULL, found, 0);
             admit = __shfl_sync(FULL, admit, 0);

@@ -136,6 +136,7 @@ struct BatchParams {
     float pad;
     unsigned long long budget_ns;
     int num_queries, num_slots, cap, path_pool_rows;
+    int admit_slots;     // slots [0, admit_slots) take new queries (max_active); the rest only extra attempts
     int edge_order;      // 0 contiguous, 1 interleaved (see warp_validate)
     long long max_samples_drawn;   // per query: max_iters x num_new_configs, pRRTC's total budget
     int sampler;         // 0 Halton lanes as pRRTC, 1 scrambled Halton per query
