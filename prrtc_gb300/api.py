@@ -404,10 +404,19 @@ class Context:
         rid = robot_id(robot)
         D, n = dof(rid), len(queries)
         trip = [q if isinstance(q, tuple) else (q.env, q.start, q.goal) for q in queries]
-        starts = np.ascontiguousarray(np.stack([np.asarray(s, np.float32).reshape(D) for _, s, _ in trip]))
-        goal_list = [np.asarray(g, np.float32).reshape(-1, D) for _, _, g in trip]
-        goals = np.ascontiguousarray(np.concatenate(goal_list))
-        ngoals = np.fromiter((len(g) for g in goal_list), np.int64, n)
+        starts = np.ascontiguousarray(np.asarray([s for _, s, _ in trip], np.float32).reshape(n, D))
+        goals = None
+        try:                                          # one goal (or k goals) per query: a single stack
+            g = np.asarray([g for _, _, g in trip], np.float32)
+            if g.ndim in (2, 3) and g.shape[0] == n and g.shape[-1] == D:
+                ngoals = np.full(n, 1 if g.ndim == 2 else g.shape[1], np.int64)
+                goals = np.ascontiguousarray(g.reshape(-1, D))
+        except ValueError:                            # ragged goal lists
+            pass
+        if goals is None:
+            goal_list = [np.asarray(g, np.float32).reshape(-1, D) for _, _, g in trip]
+            goals = np.ascontiguousarray(np.concatenate(goal_list))
+            ngoals = np.fromiter((len(g) for g in goal_list), np.int64, n)
         qs = np.zeros(n, _QUERY_DT)
         qs["start"] = starts.ctypes.data + 4 * D * np.arange(n, dtype=np.uint64)
         qs["goals"] = goals.ctypes.data + 4 * D * (np.cumsum(ngoals) - ngoals).astype(np.uint64)
@@ -419,9 +428,12 @@ class Context:
         plain = np.flatnonzero(~is_handle)
         if len(plain):
             descs = np.zeros(len(plain), _DESC_DT)
+            envs = [trip[i][0] for i in plain]
+            packed = all(type(e) is Environment for e in envs)   # float32, contiguous, [count, width] already
             for k in _ENV_KINDS:                       # one buffer per obstacle type, descriptors point into it
-                arrs = [np.asarray(getattr(trip[i][0], k), np.float32) for i in plain]
-                cnt = np.fromiter((len(a) for a in arrs), np.int64, len(arrs))
+                arrs = [getattr(e, k) for e in envs] if packed else \
+                    [np.asarray(getattr(e, k), np.float32) for e in envs]
+                cnt = np.fromiter(map(len, arrs), np.int64, len(arrs))
                 if cnt.sum():
                     buf = np.ascontiguousarray(np.concatenate(arrs))
                     keep.append(buf)
