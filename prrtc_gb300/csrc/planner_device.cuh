@@ -255,48 +255,19 @@ __device__ __forceinline__ unsigned div31(unsigned i, unsigned m, unsigned s)
     return __umulhi(i, m) >> s;
 }
 
-// Radical inverse of index i in integer base b, float32 (the closed form of
-// the reference's incremental Halton recurrence).
-__device__ __forceinline__ float radical_inverse(unsigned i, unsigned b)
-{
-    const unsigned long long s = kDivTable.magic[b];
-    const float inv = kDivTable.inv[b];
-    float f = inv, r = 0.0f;
-    while (i > 0) {
-        const unsigned q = div_by(i, s);
-        r = fmaf(f, (float)(i - q * b), r);
-        i = q;
-        f *= inv;
-    }
-    return r;
-}
-
-// Radical inverse with every digit multiplied by a (mod b), a in [1, b-1]:
-// a linear digit scrambling that breaks the correlations between the
-// sequences of large prime bases while keeping each dimension's
-// low-discrepancy structure.
-__device__ __forceinline__ float scrambled_radical_inverse(unsigned i, unsigned b, unsigned a)
-{
-    const unsigned long long s = kDivTable.magic[b];
-    const float inv = kDivTable.inv[b];
-    float f = inv, r = 0.0f;
-    while (i > 0) {
-        const unsigned q = div_by(i, s);
-        const unsigned ad = a * (i - q * b);
-        r = fmaf(f, (float)(ad - div_by(ad, s) * b), r);
-        i = q;
-        f *= inv;
-    }
-    return r;
-}
-
-// Radical inverses of one index iter < 2^31 in N bases at once (h[d] in base
-// b[d], each digit multiplied by a[d] mod b[d] when SCRAMBLE).  The digit
-// chains of the N dimensions advance together, one digit of every dimension
-// per trip, for as many trips as the smallest base needs: N independent
-// dependency chains instead of N loops in a row, and the same trip count on
-// every lane.  A dimension whose index is exhausted adds fmaf(f, 0, h) = h, so
-// every h[d] is bit-identical to radical_inverse / scrambled_radical_inverse.
+// Radical inverses of one index iter < 2^31 in N bases at once, float32: the
+// closed form of the reference's incremental Halton recurrence.  h[d] =
+// sum over the digits of iter in base b[d], least significant first, of
+// digit * b^-k, accumulated by fmaf in that order with the weight f = b^-k
+// kept as a running float product; with SCRAMBLE every digit is first
+// multiplied by a[d] mod b[d] (a linear digit scrambling that breaks the
+// correlations between large prime bases while keeping each dimension's
+// low-discrepancy structure).  The digit chains of the N dimensions advance
+// together, one digit of every dimension per trip, for as many trips as the
+// smallest base needs: N independent dependency chains instead of N loops in
+// a row, and the same trip count on every lane.  A dimension whose index is
+// exhausted adds fmaf(f, 0, h) = h, so its value is the same as from its own
+// loop.
 //
 // The state can stop between trips: after any trip, h[d] holds the digits so
 // far and the digits still to come add less than f[d] * b[d] (each at most
@@ -351,16 +322,6 @@ struct RadicalDigits {
         while (rem > 0) trip();
     }
 };
-
-template <int N, bool SCRAMBLE>
-__device__ __forceinline__ void radical_inverses(unsigned iter, const unsigned (&b)[N], const unsigned (&a)[N],
-                                                 float (&h)[N])
-{
-    RadicalDigits<N, SCRAMBLE> r(iter, b, a);
-    r.finish();
-#pragma unroll
-    for (int d = 0; d < N; d++) h[d] = r.h[d];
-}
 
 __device__ __forceinline__ unsigned hash32(unsigned x)
 {
