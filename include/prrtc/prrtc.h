@@ -244,7 +244,9 @@ typedef struct prrtc_batch_settings {
                                         own count (plan.num_new_configs) reproduces its sample set,
                                         whose first points cluster near the lower joint limits */
     int max_nodes_per_tree;          /* arena capacity per tree (0: min(max_samples, 65536)) */
-    int max_active;                  /* resident query slots (0: all queries, within the arena budget) */
+    int max_active;                  /* queries in flight at once (0: all queries, within the arena
+                                        budget); with max_attempts > 1 further slots hold only
+                                        restarts and extra attempts */
     int warps_per_block;             /* 0: 4 */
     int edge_order;                  /* order a warp checks an edge's points in: 0 contiguous
                                         rounds, 1 interleaved (every round spans the edge) */
@@ -256,8 +258,9 @@ typedef struct prrtc_batch_settings {
                                         queries running longer than k x restart_after_ns; the first
                                         attempt to connect wins */
     uint64_t restart_after_ns;       /* 0: 10 ms */
-    int max_workers_per_attempt;     /* warps working one attempt at once (0: unlimited); when every
-                                        running attempt is full, an idle warp opens a new attempt */
+    int max_workers_per_attempt;     /* warps working one attempt at once (0: unlimited; an attempt
+                                        younger than 200 us takes at most 4); when every running
+                                        attempt is full, an idle warp opens a new attempt */
     int blocks_per_sm;               /* 0: occupancy maximum */
     int use_graph;                   /* replay each run as a captured CUDA graph */
     float margin;                    /* sphere inflation while planning, metres (>= 0) */
