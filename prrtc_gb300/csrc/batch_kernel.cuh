@@ -26,11 +26,11 @@
 
 namespace prrtc {
 
-// Obstacle records a warp keeps in shared memory for the query it works on
-// (4 KB: Panda and Fetch scenes and most Baxter ones); larger scenes are
-// read from global memory through L1.
 // Per-warp shared scratch of the batched planner, followed in shared memory
-// by the warp's staged obstacle records (BatchParams::env_records of them).
+// by the obstacle records of the query the warp works on: room for the
+// batch's largest environment (BatchParams::env_records, at most
+// kWarpEnvRecords); queries with larger scenes read theirs from global
+// memory through L1.
 template <int D>
 struct alignas(16) WarpScratch {
     float from[D], step[D], cfg[D], nn[D], vec[D], next[D];
@@ -514,11 +514,11 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
     const int lane = lane_id();
     BatchCounters *C = P.ctr;
     const float fg = (float)P.granularity;
-    unsigned long long t0 = 0;   // lane 0: the launch's start (the first warp's clock)
+    unsigned long long t_launch = 0;   // lane 0: the launch's start (the first warp's clock)
     if (lane == 0) {
         const unsigned long long now = global_ns();
         const unsigned long long first = atomicCAS(&C->t0, 0ull, now);
-        t0 = first ? first : now;
+        t_launch = first ? first : now;
     }
     int slot = -1;
     int cq = 0, catt = 0;   // the slot's query and attempt, read when this warp takes the slot
@@ -534,7 +534,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
     while (true) {
         // ---- time budget
         int timed_out = 0;
-        if (lane == 0 && P.budget_ns) timed_out = global_ns() - t0 > P.budget_ns;
+        if (lane == 0 && P.budget_ns) timed_out = global_ns() - t_launch > P.budget_ns;
         timed_out = __shfl_sync(FULL, timed_out, 0);
         if (timed_out) {
             if (slot >= 0) {
