@@ -23,8 +23,10 @@ JSON line (the contract this repository's driver reads):
   cpu_baseline  the CPU restatement of pRRTC's algorithm (oracle, all host
              threads) on a bounded sample of the same queries
 
-`--impl reference` times that CPU restatement alone (the reference has no
-other runnable implementation on this machine).
+`--impl reference` times that CPU restatement alone: the reference's planner
+is not run on the GPU (its kernel writes tree nodes past max_samples and
+path entries past its fixed path array without bounds checks), so its
+algorithm restated on the CPU is the reference arm.
 """
 from __future__ import annotations
 
@@ -43,16 +45,8 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-WORKLOAD_SETTINGS = {
-    # configs[1]: Panda shelf, granularity 128, balance 2, tree_ratio 1, DD (4, 1e-4, 1); other fields default
-    "panda_shelf": dict(granularity=128, balance=2, tree_ratio=1.0, dynamic_domain=True, dd_radius=4.0,
-                        dd_alpha=1e-4, dd_min_radius=1.0),
-    # configs[0]: Panda tabletop, range 1.0, granularity 32, 256 lanes, 100k samples, balance 0, DD off
-    "panda_tabletop": dict(max_samples=100000, num_new_configs=256, granularity=32, range=1.0, balance=0,
-                           dynamic_domain=False),
-    "fetch_mixed": dict(granularity=64),
-    "baxter_mixed": dict(granularity=128, balance=1, tree_ratio=0.5),
-}
+from prrtc_gb300.workloads import SETTINGS as WORKLOAD_SETTINGS  # noqa: E402
+
 MARGIN = 1e-5   # planning margin (m): every returned path clears contact by 10 micrometres
 GPU_BUDGET_NS = int(30e9)   # per batch launch; unsolved queries past it count as failures
 CPU_BUDGET_S = 20.0         # per query in the CPU restatement
@@ -179,19 +173,25 @@ def shard_seed0(rank: int, n: int, steps: int) -> int:
     return rank * n * steps
 
 
-def reduce_over_ranks(t_dev: float, solved: int, world: int, device: str = "cpu"):
-    """Whole-job figures over ranks: the slowest rank's device time and the
-    total of solved queries (queries shard with no exchange on the data path;
-    these two numbers are the only collective)."""
+def allreduce(maxes, sums, world: int, device: str = "cpu"):
+    """Whole-job figures over ranks: elementwise maxima (times) and sums
+    (counts, bytes).  Queries shard with no exchange on the data path; these
+    figures are the only collective."""
     if world <= 1:
-        return t_dev, solved
+        return list(maxes), list(sums)
     import torch
     import torch.distributed as dist
-    t = torch.tensor([t_dev], dtype=torch.float64, device=device)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    c = torch.tensor([float(solved)], dtype=torch.float64, device=device)
+    m = torch.tensor([float(v) for v in maxes] or [0.0], dtype=torch.float64, device=device)
+    dist.all_reduce(m, op=dist.ReduceOp.MAX)
+    c = torch.tensor([float(v) for v in sums] or [0.0], dtype=torch.float64, device=device)
     dist.all_reduce(c)
-    return float(t.item()), int(c.item())
+    return m.tolist()[:len(maxes)], c.tolist()[:len(sums)]
+
+
+def reduce_over_ranks(t_dev: float, solved: int, world: int, device: str = "cpu"):
+    """The slowest rank's device time and the total of solved queries."""
+    (t,), (c,) = allreduce([t_dev], [solved], world, device)
+    return t, int(c)
 
 
 def h2d_bytes(qs):
@@ -266,6 +266,9 @@ def ours(args, rank, world):
     res_e2e = prep.results()
     e2e_solved = sum(r.solved for r in res_e2e)
     d2h = sum(len(r.path) * r.path.shape[1] * 4 for r in res_e2e) + 64 * len(res_e2e)
+    h2d = h2d_bytes(qs)
+    # whole job over ranks: the slowest rank's call, all ranks' queries and bytes
+    (e2e_t,), (e2e_solved, d2h, h2d) = allreduce([e2e_t], [e2e_solved, d2h, h2d], world, f"cuda:{dev}")
     # the same job through the Python wrapper (marshalling and unpacking timed)
     t0 = time.perf_counter()
     res_py = ctx.solve_batch(robot, host_q, bs_host, path_capacity=2048)
@@ -339,8 +342,8 @@ def ours(args, rank, world):
         "plain": {"queries_per_s": plain_qps, "p50_solve_ms": statistics.median(plain_ms),
                   "max_solve_ms": max(plain_ms), "sample": f"{ns_plain} of the first step's {n} queries",
                   "solved": plain_solved, "batched_over_plain": value / plain_qps},
-        "e2e": {"value": e2e_solved / e2e_t, "unit": "queries/s", "h2d_bytes_per_step": h2d_bytes(qs) // args.steps,
-                "d2h_bytes_per_step": d2h // args.steps, "call_ms": e2e_t * 1e3,
+        "e2e": {"value": e2e_solved / e2e_t, "unit": "queries/s", "h2d_bytes_per_step": int(h2d) // args.steps,
+                "d2h_bytes_per_step": int(d2h) // args.steps, "call_ms": e2e_t * 1e3,
                 "create_ms": res_e2e[0].copy_ns / 1e6 if res_e2e else None},
         "e2e_python": {"value": e2e_py_solved / e2e_py_t, "unit": "queries/s",
                        "note": "Context.solve_batch: the Python wrapper's marshalling and unpacking included"},
@@ -486,6 +489,16 @@ def main():
                          "they are parity cases, not the benchmark, and Baxter's launches run to a 10 s budget")
     ap.add_argument("--no-others", dest="others", action="store_false", help=argparse.SUPPRESS)
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # started without a launcher: one rank per GPU on this node
+        import socket
+        with socket.socket() as sk:
+            sk.bind(("127.0.0.1", 0))
+            port = sk.getsockname()[1]
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr", "127.0.0.1", "--master-port", str(port), str(Path(__file__).resolve()),
+               *sys.argv[1:]]
+        sys.exit(subprocess.call(cmd))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.warmup < 3:

@@ -178,8 +178,11 @@ prrtc_status prrtc_validate_edges(prrtc_ctx *ctx, prrtc_robot robot, const prrtc
  *   env        host arrays; at most PRRTC_MAX_ENV_FLOATS packed floats, else
  *              PRRTC_EINVAL (the limit of the library's fixed device array)
  *   q, out_free  device memory of the current device ([n][dof] floats, n bytes)
- *   stream     cudaStream_t to run on (NULL: the default stream); the call
- *              returns once the work is queued
+ *   stream     cudaStream_t to run on (NULL: the default stream).  The
+ *              obstacles are copied from a host array inside the library
+ *              (pageable memory); to stage that copy the driver may first
+ *              wait for the work already queued on `stream`.  The call
+ *              returns once the copy is staged and the check is queued.
  * The library keeps one fixed array of PRRTC_MAX_ENV_FLOATS floats plus two
  * counters on every GPU that loads it, for the life of the process.  Every
  * call on a device shares it, so calls whose GPU work overlaps (other
@@ -269,6 +272,9 @@ typedef struct prrtc_batch_settings {
                                         0 tightest first (smallest clearance of start or goal to an
                                         obstacle, computed on the GPU at create: the hard queries
                                         start early and no longer set the batch's end); 1 as given */
+    uint32_t idle_wait_limit;        /* polls (about 256 ns each) a warp with no work to take makes
+                                        before it gives up and the run ends with PRRTC_ECUDA and
+                                        stats.error = 1 (0: 2^22, about a second) */
 } prrtc_batch_settings;
 
 typedef struct prrtc_batch prrtc_batch;

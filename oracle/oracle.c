@@ -689,6 +689,64 @@ static int nearest(const tree_t *t, int D, const float *q, float *dsq)
     return bi;
 }
 
+/* dynamic-domain radius updates (pRRTC.cu:456-468 grow, 584-598 shrink) */
+static void dd_grow_one(float *r, float alpha)
+{
+    if (*r != FLT_MAX) *r = *r * (1.0f + alpha);
+}
+
+static void dd_shrink_one(float *r, float alpha, float radius0, float rmin)
+{
+    *r = (*r == FLT_MAX) ? radius0 : fmaxf(*r * (1.0f - alpha), rmin);
+}
+
+int oracle_halton(int dof, const float *bases16, int lanes, int steps, const float *scale, const float *offset,
+                  float *raw, float *cfg)
+{
+    if (dof < 1 || dof > 16 || lanes < 0 || steps < 0 || !bases16 || !scale || !offset || !raw || !cfg) return -1;
+    for (int l = 0; l < lanes; l++) {
+        float b[16], n[16], d[16], out[16];
+        for (int i = 0; i < dof; i++) {
+            b[i] = bases16[16 * l + i];
+            n[i] = 0.0f;
+            d[i] = 1.0f;
+        }
+        for (int s = 0; s < steps; s++) {
+            halton_next(dof, b, n, d, out);
+            const size_t o = ((size_t)l * steps + s) * dof;
+            for (int i = 0; i < dof; i++) {
+                raw[o + i] = out[i];
+                cfg[o + i] = fmaf(out[i], scale[i], offset[i]);
+            }
+        }
+    }
+    return 0;
+}
+
+int oracle_nearest(int dof, const float *nodes, int count, const float *q, int nq, int *out_i, float *out_d)
+{
+    if (dof < 1 || count < 0 || nq < 0 || (count && !nodes) || (nq && (!q || !out_i || !out_d))) return -1;
+    tree_t t;
+    memset(&t, 0, sizeof t);
+    t.nodes = (float *)nodes;
+    t.count = t.cap = count;
+    for (int k = 0; k < nq; k++) out_i[k] = nearest(&t, dof, q + (size_t)k * dof, &out_d[k]);
+    return 0;
+}
+
+int oracle_dd_apply(float *radii, int n, const uint8_t *ops, int nops, float alpha, float radius0, float rmin)
+{
+    if (n < 0 || nops < 0 || (n && (!radii || (nops && !ops)))) return -1;
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < nops; k++) {
+            if (ops[(size_t)i * nops + k])
+                dd_shrink_one(&radii[i], alpha, radius0, rmin);
+            else
+                dd_grow_one(&radii[i], alpha);
+        }
+    return 0;
+}
+
 static float trace(const tree_t *t, int D, int start, float *seg, int seg_cap, int *nseg, int *root)
 {
     float cost = 0.0f;
@@ -819,10 +877,7 @@ int oracle_solve(int robot, const float *start, const float *goals, int num_goal
                 ok = check_one(R, p, env, NULL);
             }
             if (!ok) {
-                if (S->dynamic_domain) {
-                    float *r = &T[t].radii[ni];
-                    *r = (*r == FLT_MAX) ? S->dd_radius : fmaxf(*r * (1.0f - S->dd_alpha), S->dd_min_radius);
-                }
+                if (S->dynamic_domain) dd_shrink_one(&T[t].radii[ni], S->dd_alpha, S->dd_radius, S->dd_min_radius);
                 continue;
             }
             int idx = tree_push(&T[t], D);
@@ -832,7 +887,7 @@ int oracle_solve(int robot, const float *start, const float *goals, int num_goal
             }
             T[t].parents[idx] = ni;
             T[t].radii[idx] = FLT_MAX;
-            if (S->dynamic_domain && T[t].radii[ni] != FLT_MAX) T[t].radii[ni] *= (1.0f + S->dd_alpha);
+            if (S->dynamic_domain) dd_grow_one(&T[t].radii[ni], S->dd_alpha);
             memcpy(T[t].nodes + (size_t)idx * D, cfg, sizeof(float) * D);
             /* connect */
             const int oi = nearest(&T[o], D, cfg, &dsq);

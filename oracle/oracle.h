@@ -92,6 +92,19 @@ typedef struct oracle_result {
     int64_t checks;          /* configurations checked */
 } oracle_result;
 
+/* Units of the planner, for the device-side parity tests:
+ *   oracle_halton    lanes x steps points of halton_next (pRRTC.cu:81-105) from
+ *                    bases16[lane][16] (the lane's primes), raw and scaled by
+ *                    fmaf(raw, scale, offset) (Robot::scale_cfg, Robots.hh);
+ *   oracle_nearest   argmin of squared L2 (sq_l2_dist, utils.cuh:100-109) over
+ *                    nodes[count][dof], first index on ties, NaN nodes never win;
+ *   oracle_dd_apply  ops[i][k] (0 grow, 1 shrink) applied in order to radii[i]
+ *                    (pRRTC.cu:456-468, 584-598). */
+int oracle_halton(int dof, const float *bases16, int lanes, int steps, const float *scale, const float *offset,
+                  float *raw, float *cfg);
+int oracle_nearest(int dof, const float *nodes, int count, const float *q, int nq, int *out_i, float *out_d);
+int oracle_dd_apply(float *radii, int n, const uint8_t *ops, int nops, float alpha, float radius0, float rmin);
+
 int oracle_solve(int robot, const float *start, const float *goals, int num_goals, const oracle_env *env,
                  const oracle_settings *s, const float *bases, float *path, int path_cap, oracle_result *res);
 

@@ -53,7 +53,15 @@ class _EnvRef:
 
 
 def build(ref: bool = False):
-    subprocess.run(["make", "-s", "-C", str(HERE)] + (["ref"] if ref else []), check=True)
+    """make the oracle (and the reference checker), holding a file lock so
+    that processes starting together build once."""
+    import fcntl
+    with open(HERE / ".build.lock", "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            subprocess.run(["make", "-s", "-C", str(HERE)] + (["ref"] if ref else []), check=True)
+        finally:
+            fcntl.flock(lock, fcntl.LOCK_UN)
 
 
 class OracleLib:
@@ -70,6 +78,10 @@ class OracleLib:
         self.L.oracle_fk_spheres.argtypes = [C.c_int, C.c_void_p, C.c_long, C.c_void_p]
         self.L.oracle_solve.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(OEnv), C.POINTER(OSettings),
                                         C.c_void_p, C.c_void_p, C.c_int, C.POINTER(OResult)]
+        self.L.oracle_halton.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p]
+        self.L.oracle_nearest.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        self.L.oracle_dd_apply.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float]
         self.L.oracle_solve_many.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(OSettings),
                                              C.c_void_p, C.c_int, C.c_void_p, C.c_int]
 
@@ -127,6 +139,35 @@ class OracleLib:
         out = np.empty((len(q), S, 4), np.float64)
         assert self.L.oracle_fk_spheres(ROBOTS[robot], q.ctypes.data, len(q), out.ctypes.data) == 0
         return out
+
+    def halton(self, bases16, steps, scale, offset):
+        """halton_next per lane from bases16 [lanes, 16]: (raw, scaled), each [lanes, steps, dof]."""
+        D = len(scale)
+        b = np.ascontiguousarray(np.asarray(bases16, np.float32).reshape(-1, 16))
+        sc = np.ascontiguousarray(np.asarray(scale, np.float32))
+        of = np.ascontiguousarray(np.asarray(offset, np.float32))
+        raw = np.empty((len(b), steps, D), np.float32)
+        cfg = np.empty_like(raw)
+        assert self.L.oracle_halton(D, b.ctypes.data, len(b), steps, sc.ctypes.data, of.ctypes.data, raw.ctypes.data,
+                                    cfg.ctypes.data) == 0
+        return raw, cfg
+
+    def nearest(self, nodes, q):
+        """(index, squared distance) of the nearest of nodes [count, dof] to each row of q."""
+        nodes = np.ascontiguousarray(np.asarray(nodes, np.float32))
+        q = np.ascontiguousarray(np.asarray(q, np.float32).reshape(-1, nodes.shape[1]))
+        oi = np.empty(len(q), np.int32)
+        od = np.empty(len(q), np.float32)
+        assert self.L.oracle_nearest(nodes.shape[1], nodes.ctypes.data, len(nodes), q.ctypes.data, len(q),
+                                     oi.ctypes.data, od.ctypes.data) == 0
+        return oi, od
+
+    def dd_apply(self, radii, ops, alpha, radius0, rmin):
+        """Radii after applying ops [n, k] (0 grow, 1 shrink) in order."""
+        r = np.array(radii, np.float32)
+        ops = np.ascontiguousarray(np.asarray(ops, np.uint8).reshape(len(r), -1))
+        assert self.L.oracle_dd_apply(r.ctypes.data, len(r), ops.ctypes.data, ops.shape[1], alpha, radius0, rmin) == 0
+        return r
 
     @staticmethod
     def settings(s, budget_s: float = 0.0) -> OSettings:
@@ -192,3 +233,144 @@ class RefLib:
                                                              out.ctypes.data)
         assert rc == 0
         return out
+
+
+class _Cubin:
+    """A cubin built here from the reference sources, loaded through the CUDA
+    driver API into the current (torch's primary) context; kernels launch on
+    torch's current stream with device pointers from torch tensors."""
+
+    _CU = None
+
+    def __init__(self, path: Path, names):
+        import torch
+        self.torch = torch
+        torch.zeros(1, device="cuda")          # make torch's primary context current
+        cu = self._driver()
+        self.mod = C.c_void_p()
+        self._ok(cu.cuModuleLoad(C.byref(self.mod), str(path).encode()), f"cuModuleLoad {path.name}")
+        self.fn = {}
+        for name in names:
+            f = C.c_void_p()
+            self._ok(cu.cuModuleGetFunction(C.byref(f), self.mod, name.encode()), name)
+            self.fn[name] = f
+
+    @classmethod
+    def _driver(cls):
+        if cls._CU is None:
+            cu = C.CDLL("libcuda.so.1")
+            for f in ("cuModuleLoad", "cuModuleGetFunction", "cuLaunchKernel"):
+                getattr(cu, f).restype = C.c_int
+            cu.cuModuleLoad.argtypes = [C.POINTER(C.c_void_p), C.c_char_p]
+            cu.cuModuleGetFunction.argtypes = [C.POINTER(C.c_void_p), C.c_void_p, C.c_char_p]
+            cu.cuLaunchKernel.argtypes = [C.c_void_p, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_uint,
+                                          C.c_uint, C.c_void_p, C.c_void_p, C.c_void_p]
+            cls._CU = cu
+        return cls._CU
+
+    @staticmethod
+    def _ok(rc, what):
+        if rc != 0:
+            raise RuntimeError(f"{what} failed: CUresult {rc}")
+
+    def launch(self, name, grid, block, args):
+        stream = self.torch.cuda.current_stream().cuda_stream
+        ptrs = (C.c_void_p * len(args))(*[C.cast(C.pointer(a), C.c_void_p) for a in args])
+        self._ok(self._driver().cuLaunchKernel(self.fn[name], grid, 1, 1, block, 1, 1, 0, C.c_void_p(stream), ptrs,
+                                               None), f"cuLaunchKernel {name}")
+
+
+class RefGpuChecker(_Cubin):
+    """pRRTC's own GPU checker: fkcc<Robot> (utils.cuh:326-327) in the harness
+    kernels of oracle/ref_fkcc_gpu.cu, one sm_103a cubin per robot built by
+    `make -C oracle ref_gpu`.  Each check builds the reference's
+    Environment<float> on the device, then runs one configuration per
+    thread."""
+
+    def __init__(self, robot: str):
+        self.kname = f"ref_fkcc_gpu_{REF_NAMES[robot]}"
+        super().__init__(self.path(robot), (self.kname, "ref_env_build", "ref_env_bytes"))
+        torch = self.torch
+        self.dim = {"sphere": 3, "panda": 7, "fetch": 8, "baxter": 14}[robot]
+        sizes = torch.zeros(5, dtype=torch.int64, device="cuda")
+        self.launch("ref_env_bytes", 1, 1, [C.c_void_p(sizes.data_ptr())])
+        torch.cuda.synchronize()
+        self.sizes = [int(v) for v in sizes.cpu()]   # Environment, Sphere, Capsule, Cuboid sizes; alignment
+        assert self.sizes[4] <= 256
+
+    @staticmethod
+    def path(robot: str) -> Path:
+        return HERE / "_ref" / f"ref_fkcc_gpu_{REF_NAMES[robot]}.cubin"
+
+    @classmethod
+    def available(cls, robot: str) -> bool:
+        return cls.path(robot).exists()
+
+    def check(self, env, q) -> np.ndarray:
+        """Reference verdicts (1 = free) for configurations q [n, dof]."""
+        torch = self.torch
+        q = torch.from_numpy(_arr(q, self.dim)).cuda()
+        arrs = [torch.from_numpy(_arr(a, k)).cuda() for a, k in
+                ((env.spheres, 4), (env.capsules, 8), (env.z_aligned_capsules, 8), (env.cuboids, 15),
+                 (env.z_aligned_cuboids, 15))]
+        per = [self.sizes[1], self.sizes[2], self.sizes[2], self.sizes[3], self.sizes[3]]
+
+        def r256(b):
+            return (b + 255) // 256 * 256
+
+        nbytes = r256(self.sizes[0]) + sum(r256(p * len(a)) for p, a in zip(per, arrs))
+        scratch = torch.zeros(nbytes + 256, dtype=torch.uint8, device="cuda")
+        assert scratch.data_ptr() % 256 == 0
+        eargs = [C.c_void_p(scratch.data_ptr())]
+        for a in arrs:
+            eargs += [C.c_void_p(a.data_ptr() if len(a) else 0), C.c_int(len(a))]
+        self.launch("ref_env_build", 1, 1, eargs)
+        n = len(q)
+        out = torch.full((max(n, 1),), 255, dtype=torch.uint8, device="cuda")
+        if n:
+            self.launch(self.kname, (n + 127) // 128, 128,
+                        [C.c_void_p(q.data_ptr()), C.c_longlong(n), C.c_int(self.dim),
+                         C.c_void_p(scratch.data_ptr()), C.c_void_p(out.data_ptr())])
+        torch.cuda.synchronize()
+        res = out[:n].cpu().numpy()
+        assert np.all(res <= 1), "reference GPU checker left verdicts unwritten"
+        return res
+
+
+class RefSampler(_Cubin):
+    """pRRTC's own sampler (oracle/ref_planner_gpu.cu, which includes
+    pRRTC.cu unmodified; `make -C oracle ref_sampler`): the reference's
+    init_rng kernel (pRRTC.cu:107-111, seed 1 as pRRTC::solve passes it),
+    then halton_initialize / halton_next / scale_cfg for every lane."""
+
+    PATH = HERE / "_ref" / "ref_sampler.cubin"
+    INIT_RNG = "_ZN6pRRTC8init_rngEP17curandStateXORWOWmi"   # pRRTC::init_rng(curandState*, unsigned long, int)
+
+    def __init__(self):
+        super().__init__(self.PATH, [self.INIT_RNG, "ref_curand_state_bytes"] +
+                         [f"ref_halton_{r}" for r in REF_NAMES.values()])
+        torch = self.torch
+        sz = torch.zeros(1, dtype=torch.int64, device="cuda")
+        self.launch("ref_curand_state_bytes", 1, 1, [C.c_void_p(sz.data_ptr())])
+        torch.cuda.synchronize()
+        self.state_bytes = int(sz.item())
+
+    @classmethod
+    def available(cls) -> bool:
+        return cls.PATH.exists()
+
+    def run(self, robot: str, lanes: int, steps: int):
+        """(bases [lanes, dof], raw [lanes, steps, dof], scaled [lanes, steps, dof])."""
+        torch = self.torch
+        D = {"sphere": 3, "panda": 7, "fetch": 8, "baxter": 14}[robot]
+        states = torch.zeros(lanes * self.state_bytes + 256, dtype=torch.uint8, device="cuda")
+        self.launch(self.INIT_RNG, (lanes + 63) // 64, 64,
+                    [C.c_void_p(states.data_ptr()), C.c_ulong(1), C.c_int(lanes)])
+        bases = torch.empty((lanes, D), dtype=torch.float32, device="cuda")
+        raw = torch.empty((lanes, steps, D), dtype=torch.float32, device="cuda")
+        cfg = torch.empty_like(raw)
+        self.launch(f"ref_halton_{REF_NAMES[robot]}", (lanes + 63) // 64, 64,
+                    [C.c_void_p(states.data_ptr()), C.c_void_p(bases.data_ptr()), C.c_void_p(raw.data_ptr()),
+                     C.c_void_p(cfg.data_ptr()), C.c_int(lanes), C.c_int(steps)])
+        torch.cuda.synchronize()
+        return bases.cpu().numpy(), raw.cpu().numpy(), cfg.cpu().numpy()

@@ -84,7 +84,8 @@ class BatchSettings(C.Structure):
                 ("max_attempts", C.c_int), ("restart_after_ns", C.c_uint64), ("max_workers_per_attempt", C.c_int),
                 ("blocks_per_sm", C.c_int),
                 ("use_graph", C.c_int),
-                ("margin", C.c_float), ("time_budget_ns", C.c_uint64), ("admission", C.c_int)]
+                ("margin", C.c_float), ("time_budget_ns", C.c_uint64), ("admission", C.c_int),
+                ("idle_wait_limit", C.c_uint32)]
 
     def __init__(self, plan: Settings | None = None, **kw):
         super().__init__()

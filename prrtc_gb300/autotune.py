@@ -12,12 +12,15 @@ Sweeps, on a calibration batch of seeded queries, the knobs of
                        Halton;
 * ``max_workers_per_attempt``  warps per attempt before idle warps open
                        independent attempts (the tail's portfolio);
-* ``max_attempts``     attempts per query, fixed at 4: restarting an attempt
-                       that exhausted its arena costs nothing until it happens,
-                       so it is a robustness setting rather than a speed knob;
+* ``max_attempts``     attempts per query, 1 (pRRTC's behaviour: a query whose
+                       attempt fails stays unsolved) or 4 (an attempt that
+                       exhausts its samples or arena restarts the query);
 
-and keeps the setting with the highest solved queries per second.  Results
-are cached in ``tuning.json`` next to this file, keyed by robot and workload:
+and keeps the setting with the highest solved queries per second among those
+that solve the most queries.  Results are cached in ``tuning.json`` next to
+this file, keyed by robot and workload; each entry's ``source`` says whether
+its ``best`` is the sweep's winner ("sweep") or was set by hand after
+longer measurements than the sweep makes ("hand-set", with a ``note``):
 
     python -m prrtc_gb300.autotune panda_shelf [queries] [budget_s]   # on a GPU; rewrites the entry
 """
@@ -73,14 +76,12 @@ def tune(ctx, robot, queries, plan, margin=1e-5, reps=3, space=None, budget_ns=i
                      "queries_per_s": min(solved) / (med * 1e-3)})
     top = max(r["solved"] for r in rows)
     best = max((r for r in rows if r["solved"] == top), key=lambda r: r["queries_per_s"])
-    return {"best": {k: best[k] for k in KNOBS}, "sweep": rows}
+    return {"best": {k: best[k] for k in KNOBS}, "source": "sweep", "sweep": rows}
 
 
 def main(argv):
     from . import workloads
     from .api import Context, Settings
-    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
-    from bench import WORKLOAD_SETTINGS   # the benchmark's settings per workload
     name = argv[1] if len(argv) > 1 else "panda_shelf"
     n = int(argv[2]) if len(argv) > 2 else 1024
     budget_s = float(argv[3]) if len(argv) > 3 else 60.0
@@ -88,7 +89,7 @@ def main(argv):
     qs = workloads.make(name, n, seed0=100_000)    # calibration queries, disjoint from the benchmark's
     ctx = Context(0)
     envs = [ctx.upload_env(q.env) for q in qs]
-    out = tune(ctx, robot, [(e, q.start, q.goal) for e, q in zip(envs, qs)], Settings(**WORKLOAD_SETTINGS[name]),
+    out = tune(ctx, robot, [(e, q.start, q.goal) for e, q in zip(envs, qs)], Settings(**workloads.SETTINGS[name]),
                budget_ns=int(budget_s * 1e9))
     table = json.loads(TUNING.read_text()) if TUNING.exists() else {}
     table[f"{robot}/{name}"] = out

@@ -1,10 +1,13 @@
 """Compile the library (sm_103a) in-tree: prrtc_gb300/libprrtc_gb300.so.
 
 Each .cu under csrc/ is one nvcc job (the per-robot kernel files dominate);
-jobs run in parallel and only out-of-date objects are rebuilt.
+jobs run in parallel and only out-of-date objects are rebuilt.  The build
+holds an exclusive file lock (_build/.lock), so processes that start together
+(one per GPU) build once and the others wait for it.
 """
 from __future__ import annotations
 
+import fcntl
 import os
 import subprocess
 import sys
@@ -44,6 +47,15 @@ def _compile(src: str, hdr_time: float, verbose: bool) -> str:
 
 def build(verbose: bool = False) -> Path:
     OBJ.mkdir(exist_ok=True)
+    with open(OBJ / ".lock", "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            return _build_locked(verbose)
+        finally:
+            fcntl.flock(lock, fcntl.LOCK_UN)
+
+
+def _build_locked(verbose: bool) -> Path:
     hdr = _deps()
     jobs = min(len(SOURCES), os.cpu_count() or 4)
     with ThreadPoolExecutor(jobs) as ex:
@@ -54,10 +66,12 @@ def build(verbose: bool = False) -> Path:
                 print(msg, file=sys.stderr)
     objs = [str(OBJ / (Path(s).stem + ".o")) for s in SOURCES]
     if not LIB.exists() or LIB.stat().st_mtime < max(Path(o).stat().st_mtime for o in objs):
-        cmd = [NVCC, *ARCH, "-shared", "-o", str(LIB), *objs, "-lcudart"]
+        tmp = LIB.with_suffix(".so.tmp")
+        cmd = [NVCC, *ARCH, "-shared", "-o", str(tmp), *objs, "-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        tmp.replace(LIB)   # a process that has the old library loaded keeps its mapping
     return LIB
 
 

@@ -645,7 +645,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                     flush();
                     return;
                 }
-                if (++idle > (1u << 22)) {
+                if (++idle > P.idle_limit) {
                     if (lane == 0) atomicOr(&C->error, 1);
                     flush();
                     return;

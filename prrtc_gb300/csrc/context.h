@@ -16,19 +16,20 @@ struct Env {
     uint32_t num_cylinders = 0;      // accepted, never checked (as the reference)
 };
 
-// Pack a flat obstacle description into float4 records (layout in device_common.cuh).
-inline void pack_env(const prrtc_env_desc &d, std::vector<float4> &out)
+// Pack a flat obstacle description into float4 records (layout in
+// device_common.cuh), handing each record to emit(float4) in order.
+template <class Emit>
+inline void pack_records(const prrtc_env_desc &d, Emit &&emit)
 {
-    out.clear();
     for (uint32_t i = 0; i < d.num_spheres; i++) {
         const float *s = d.spheres + 4 * i;
-        out.push_back(make_float4(s[0], s[1], s[2], s[3]));
+        emit(make_float4(s[0], s[1], s[2], s[3]));
     }
     auto caps = [&](const float *p, uint32_t n) {
         for (uint32_t i = 0; i < n; i++) {
             const float *c = p + 8 * i;
-            out.push_back(make_float4(c[0], c[1], c[2], c[6]));
-            out.push_back(make_float4(c[3], c[4], c[5], c[7]));
+            emit(make_float4(c[0], c[1], c[2], c[6]));
+            emit(make_float4(c[3], c[4], c[5], c[7]));
         }
     };
     caps(d.capsules, d.num_capsules);
@@ -36,14 +37,20 @@ inline void pack_env(const prrtc_env_desc &d, std::vector<float4> &out)
     auto cubs = [&](const float *p, uint32_t n) {
         for (uint32_t i = 0; i < n; i++) {
             const float *c = p + 15 * i;
-            out.push_back(make_float4(c[0], c[1], c[2], c[12]));
-            out.push_back(make_float4(c[3], c[4], c[5], c[13]));
-            out.push_back(make_float4(c[6], c[7], c[8], c[14]));
-            out.push_back(make_float4(c[9], c[10], c[11], 0.0f));
+            emit(make_float4(c[0], c[1], c[2], c[12]));
+            emit(make_float4(c[3], c[4], c[5], c[13]));
+            emit(make_float4(c[6], c[7], c[8], c[14]));
+            emit(make_float4(c[9], c[10], c[11], 0.0f));
         }
     };
     cubs(d.cuboids, d.num_cuboids);
     cubs(d.z_aligned_cuboids, d.num_z_aligned_cuboids);
+}
+
+inline void pack_env(const prrtc_env_desc &d, std::vector<float4> &out)
+{
+    out.clear();
+    pack_records(d, [&](float4 r) { out.push_back(r); });
 }
 
 struct PlannerState;    // planner.cu

@@ -9,7 +9,10 @@
 // storage is the file-scope array below (kScratchBytes, reserved on every GPU
 // that loads the library until the process exits): the packed obstacles of
 // the call and the checker's two work counters.  The caller provides the
-// configurations and the verdict buffer in device memory.
+// configurations and the verdict buffer in device memory.  The obstacles are
+// packed into a file-scope host array and copied from there; to stage a copy
+// from pageable memory the driver may first wait for the work already queued
+// on the stream.
 //
 // The array is shared by every call on a device and keeps the last call's
 // contents; the counters are cleared at the start of each call.  Two calls
@@ -64,36 +67,12 @@ prrtc_status scratch_on_current_device(void **ptr, int *sms)
     return PRRTC_OK;
 }
 
-// Pack into a caller-stack buffer (no heap): same layout as prrtc_env_upload.
-size_t pack_flat(const prrtc_env_desc &d, float4 *out)
-{
-    size_t k = 0;
-    for (uint32_t i = 0; i < d.num_spheres; i++) {
-        const float *s = d.spheres + 4 * i;
-        out[k++] = make_float4(s[0], s[1], s[2], s[3]);
-    }
-    auto caps = [&](const float *p, uint32_t n) {
-        for (uint32_t i = 0; i < n; i++) {
-            const float *c = p + 8 * i;
-            out[k++] = make_float4(c[0], c[1], c[2], c[6]);
-            out[k++] = make_float4(c[3], c[4], c[5], c[7]);
-        }
-    };
-    caps(d.capsules, d.num_capsules);
-    caps(d.z_aligned_capsules, d.num_z_aligned_capsules);
-    auto cubs = [&](const float *p, uint32_t n) {
-        for (uint32_t i = 0; i < n; i++) {
-            const float *c = p + 15 * i;
-            out[k++] = make_float4(c[0], c[1], c[2], c[12]);
-            out[k++] = make_float4(c[3], c[4], c[5], c[13]);
-            out[k++] = make_float4(c[6], c[7], c[8], c[14]);
-            out[k++] = make_float4(c[9], c[10], c[11], 0.0f);
-        }
-    };
-    cubs(d.cuboids, d.num_cuboids);
-    cubs(d.z_aligned_cuboids, d.num_z_aligned_cuboids);
-    return k;
-}
+// The packed obstacles of the call being made: a file-scope host array (no
+// heap, nothing on the caller's stack), guarded while a call packs and
+// copies it.  A copy from pageable memory returns once the data is staged,
+// so the array is free again when cudaMemcpyAsync returns.
+float4 g_packed[PRRTC_MAX_ENV_FLOATS / 4];
+std::mutex g_pack_mu;
 
 }  // namespace
 
@@ -116,13 +95,17 @@ extern "C" prrtc_status prrtc_validate_configs_noalloc(prrtc_robot robot, const 
     prrtc_status s = scratch_on_current_device(&scratch, &sms);
     if (s) return s;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    float4 packed[PRRTC_MAX_ENV_FLOATS / 4];
-    const size_t rec = pack_flat(*env, packed);
     unsigned long long *work = reinterpret_cast<unsigned long long *>(static_cast<unsigned char *>(scratch) + kEnvBytes);
-    if ((rec && cudaMemcpyAsync(scratch, packed, rec * sizeof(float4), cudaMemcpyHostToDevice, st) != cudaSuccess) ||
-        cudaMemsetAsync(work, 0, 2 * sizeof(unsigned long long), st) != cudaSuccess) {
-        cudaGetLastError();
-        return PRRTC_ECUDA;
+    {
+        std::lock_guard<std::mutex> g(g_pack_mu);
+        size_t rec = 0;
+        prrtc::pack_records(*env, [&](float4 r) { g_packed[rec++] = r; });   // rec <= PRRTC_MAX_ENV_FLOATS / 4
+        if ((rec && cudaMemcpyAsync(scratch, g_packed, rec * sizeof(float4), cudaMemcpyHostToDevice, st) !=
+                        cudaSuccess) ||
+            cudaMemsetAsync(work, 0, 2 * sizeof(unsigned long long), st) != cudaSuccess) {
+            cudaGetLastError();
+            return PRRTC_ECUDA;
+        }
     }
     const prrtc::EnvCounts counts{(int)env->num_spheres, (int)env->num_capsules, (int)env->num_z_aligned_capsules,
                                   (int)env->num_cuboids, (int)env->num_z_aligned_cuboids};

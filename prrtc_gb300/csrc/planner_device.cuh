@@ -45,6 +45,16 @@ __device__ __forceinline__ void halton_next(float *b, float *n, float *d, float 
     }
 }
 
+// A raw Halton point scaled into the joint box as Robot::scale_cfg does
+// (Robots.hh: q * s_m + s_a, one fused multiply-add per joint, as nvcc
+// contracts it).
+template <int D>
+__device__ __forceinline__ void scale_sample(float *q, const float *scale, const float *offset)
+{
+#pragma unroll
+    for (int d = 0; d < D; d++) q[d] = fmaf(q[d], scale[d], offset[d]);
+}
+
 // Block-wide nearest neighbour of s_q among the first `count` nodes of a tree.
 // Squared L2 accumulated as the reference does (sq_l2_dist, utils.cuh:100-109).
 // Ties resolve to the lowest node index.  Result in (s_out_d, s_out_i).
@@ -108,11 +118,16 @@ __device__ __forceinline__ void block_nn(const float *__restrict__ nodes, int ca
 }
 
 // Dynamic-domain updates with the reference's CAS loops (pRRTC.cu:456-468,
-// 584-598), bounded so a contended radius cannot spin forever.
+// 584-598).  A failed CAS means another update landed, so every update ends
+// after at most as many retries as there are concurrent updaters; the loop is
+// still bounded (kDdTries, far above any block or warp count the planners
+// launch) so that no wait can be endless.
+constexpr int kDdTries = 1 << 16;
+
 __device__ __forceinline__ void dd_grow(float *r, float alpha)
 {
     volatile float *rp = r;
-    for (int tries = 0; tries < 256; tries++) {
+    for (int tries = 0; tries < kDdTries; tries++) {
         const float old = *rp;
         if (old == FLT_MAX) return;
         const float nw = old * (1.0f + alpha);
@@ -123,7 +138,7 @@ __device__ __forceinline__ void dd_grow(float *r, float alpha)
 __device__ __forceinline__ void dd_shrink(float *r, float alpha, float radius0, float rmin)
 {
     volatile float *rp = r;
-    for (int tries = 0; tries < 256; tries++) {
+    for (int tries = 0; tries < kDdTries; tries++) {
         const float old = *rp;
         const float nw = (old == FLT_MAX) ? radius0 : fmaxf(old * (1.0f - alpha), rmin);
         if (atomicCAS(reinterpret_cast<int *>(r), __float_as_int(old), __float_as_int(nw)) == __float_as_int(old)) return;

@@ -144,6 +144,7 @@ struct BatchParams {
     int max_workers;     // warps per attempt
     int bases_lanes;     // rows of halton_bases
     unsigned long long restart_after_ns;   // a query may get its k-th extra attempt after k x this
+    unsigned idle_limit;                   // polls before an idle warp gives up (error flag)
     const float *cfg_pool;
     const BatchQueryDesc *queries;
     const int *order;    // admission order (query ids), null: index order

@@ -203,8 +203,7 @@ __global__ void __launch_bounds__(256) k_rrtc_plain(const PlainParams P)
             }
             s_o = 1 - s_t;
             halton_next<D>(s_hb, s_hn, s_hd, s_cfg);
-#pragma unroll
-            for (int d = 0; d < D; d++) s_cfg[d] = fmaf(s_cfg[d], P.scale[d], P.offset[d]);
+            scale_sample<D>(s_cfg, P.scale, P.offset);
         }
         __syncthreads();
         const int t = s_t, o = s_o;

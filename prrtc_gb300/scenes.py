@@ -75,14 +75,45 @@ class Rng:
 
 # ------------------------------------------------------------------- scenes
 
+def _z_one(rng: Rng, capsule: bool, lo, hi, floor_z=None):
+    """One z-aligned obstacle centred uniformly in [lo, hi] (standing on the
+    plane z = floor_z when given): a vertical capsule (r U[0.02, 0.05],
+    length U[0.1, 0.3]) or a yawed box (half-extents U[0.02, 0.10], yaw
+    U[-pi, pi]).  These are the reference's z_aligned_capsules and
+    z_aligned_cuboids (environment.hh:20-30), which its checker tests with
+    sphere_z_aligned_capsule / sphere_z_aligned_cuboid (utils.cuh:134-148,
+    178-197): only the axis' z (capsule) or the axes' x, y (box) are read."""
+    c = rng.uniform(np.asarray(lo, np.float64), np.asarray(hi, np.float64), (3,))
+    if capsule:
+        r = rng.uniform(0.02, 0.05)
+        h = rng.uniform(0.1, 0.3)
+        z0 = floor_z + r if floor_z is not None else c[2] - h / 2
+        return capsule_row((c[0], c[1], z0 + h), (c[0], c[1], z0), r)
+    half = rng.uniform(0.02, 0.10, (3,))
+    yaw = rng.uniform(-np.pi, np.pi)
+    if floor_z is not None:
+        c[2] = floor_z + half[2]
+    return cuboid_row(c, half, (0.0, 0.0, yaw))
+
+
+def _z_extras(rng: Rng, n: int, lo, hi, floor_z=None):
+    """n z-aligned obstacles, alternating capsule and box (see _z_one)."""
+    rows = [_z_one(rng, k % 2 == 0, lo, hi, floor_z) for k in range(n)]
+    zc = np.array([r for r in rows if len(r) == 8], np.float32).reshape(-1, 8)
+    zb = np.array([r for r in rows if len(r) == 15], np.float32).reshape(-1, 15)
+    return zc, zb
+
+
 TABLE_CENTER = (0.8, 0.0, 0.4)
 TABLE_HALF = (0.5, 0.4, 0.025)
 
 
-def tabletop_scene(seed: int, z_offset: float = 0.0, n_spheres: int = 8, n_boxes: int = 4) -> Environment:
+def tabletop_scene(seed: int, z_offset: float = 0.0, n_spheres: int = 8, n_boxes: int = 4,
+                   n_zaligned: int = 0) -> Environment:
     """Table (1.0 x 0.8 x 0.05 m cuboid, top at z=0.425) with spheres of radius
     U[0.03, 0.08] and axis-aligned boxes of half-extents U[0.02, 0.10] placed
-    uniformly in the 0.8 m cube above it."""
+    uniformly in the 0.8 m cube above it; plus n_zaligned z-aligned obstacles
+    (vertical capsules and yawed boxes) standing on the table."""
     rng = Rng(seed)
     lo = np.array([0.4, -0.4, 0.425 + z_offset])
     hi = lo + 0.8
@@ -92,7 +123,11 @@ def tabletop_scene(seed: int, z_offset: float = 0.0, n_spheres: int = 8, n_boxes
         c = rng.uniform(lo, hi, (3,))
         h = rng.uniform(0.02, 0.10, (3,))
         boxes.append(cuboid_row(c, h))
-    return Environment(spheres=np.array(sph, np.float32), cuboids=np.array(boxes, np.float32))
+    tc = np.array(TABLE_CENTER) + [0, 0, z_offset]
+    top = tc[2] + TABLE_HALF[2]
+    zc, zb = _z_extras(rng, n_zaligned, tc - [0.45, 0.35, 0.0], tc + [0.45, 0.35, 0.0], floor_z=top)
+    return Environment(spheres=np.array(sph, np.float32), cuboids=np.array(boxes, np.float32),
+                       z_aligned_capsules=zc, z_aligned_cuboids=zb)
 
 
 SHELF_FRONT_X, SHELF_DEPTH, SHELF_BOTTOM, CELL, WALL = 0.55, 0.30, 0.30, 0.25, 0.02
@@ -111,12 +146,14 @@ def shelf_cells(z_offset: float = 0.0):
     return cells
 
 
-def shelf_scene(seed: int, z_offset: float = 0.0, n_cyl: int = 12, n_sph: int = 20) -> Environment:
+def shelf_scene(seed: int, z_offset: float = 0.0, n_cyl: int = 12, n_sph: int = 20, n_zaligned: int = 0) -> Environment:
     """3x3 shelf of 0.25 m cells with 0.02 m boards (4 shelves, 4 dividers and
     a back plate: 9 cuboids; front face x=0.55, depth 0.30, bottom z=0.30),
     plus vertical cylinders (r U[0.02, 0.05], h U[0.1, 0.3], random yaw;
     stored as capsules, as the reference's MBM loader stores cylinders) and
-    spheres (r U[0.03, 0.08]) standing in random cells."""
+    spheres (r U[0.03, 0.08]) standing in random cells; plus n_zaligned
+    z-aligned obstacles (vertical capsules, yawed boxes) standing on the
+    boards of random cells."""
     rng = Rng(seed)
     pitch = CELL + WALL
     width = 3 * CELL + 4 * WALL
@@ -146,13 +183,20 @@ def shelf_scene(seed: int, z_offset: float = 0.0, n_cyl: int = 12, n_sph: int = 
         lo, hi = cells[rng.integers(0, 8)]
         r = rng.uniform(0.03, 0.08)
         sph.append([*rng.uniform(lo + r, hi - r, (3,)), r])
+    zc, zb = [], []
+    for k in range(n_zaligned):
+        lo, hi = cells[rng.integers(0, 8)]
+        row = _z_one(rng, k % 2 == 0, lo + 0.05, hi - 0.05, floor_z=lo[2])
+        (zc if len(row) == 8 else zb).append(row)
     return Environment(spheres=np.array(sph, np.float32), capsules=np.array(caps, np.float32),
-                       cuboids=np.array(boxes, np.float32))
+                       cuboids=np.array(boxes, np.float32), z_aligned_capsules=np.array(zc, np.float32).reshape(-1, 8),
+                       z_aligned_cuboids=np.array(zb, np.float32).reshape(-1, 15))
 
 
-def mixed_scene(seed: int, n_obstacles: int, lo=(0.5, -0.4, 0.5), hi=(1.3, 0.4, 1.3)) -> Environment:
+def mixed_scene(seed: int, n_obstacles: int, lo=(0.5, -0.4, 0.5), hi=(1.3, 0.4, 1.3), n_zaligned: int = 0) -> Environment:
     """n obstacles of uniformly drawn type (sphere, cuboid, capsule), sizes as
-    the tabletop scene, placed uniformly in the box [lo, hi]."""
+    the tabletop scene, placed uniformly in the box [lo, hi]; plus n_zaligned
+    z-aligned obstacles (vertical capsules, yawed boxes) in the same box."""
     rng = Rng(seed)
     lo, hi = np.array(lo), np.array(hi)
     sph, box, cap = [], [], []
@@ -169,8 +213,9 @@ def mixed_scene(seed: int, n_obstacles: int, lo=(0.5, -0.4, 0.5), hi=(1.3, 0.4, 
             caps_dir = rng.uniform(-1.0, 1.0, (3,))
             caps_dir /= max(np.linalg.norm(caps_dir), 1e-9)
             cap.append(capsule_row(c - caps_dir * h / 2, c + caps_dir * h / 2, r))
+    zc, zb = _z_extras(rng, n_zaligned, lo, hi)
     return Environment(spheres=np.array(sph, np.float32).reshape(-1, 4), cuboids=np.array(box, np.float32).reshape(-1, 15),
-                       capsules=np.array(cap, np.float32).reshape(-1, 8))
+                       capsules=np.array(cap, np.float32).reshape(-1, 8), z_aligned_capsules=zc, z_aligned_cuboids=zb)
 
 
 # ------------------------------------------------------ clearance (float64)
@@ -282,15 +327,17 @@ def in_cell(robot: str, q: np.ndarray, cell) -> np.ndarray:
     return np.all((c >= lo) & (c <= hi), axis=-1)
 
 
-def make_query(robot: str, kind: str, seed: int, n_obstacles: int | None = None, z_offset: float = 0.0) -> Query:
+def make_query(robot: str, kind: str, seed: int, n_obstacles: int | None = None, z_offset: float = 0.0,
+               n_zaligned: int = 0) -> Query:
     """One seeded query.  kind: 'tabletop', 'shelf' (goal: hand inside a cell)
-    or 'mixed' (n_obstacles of mixed types)."""
+    or 'mixed' (n_obstacles of mixed types); n_zaligned adds that many
+    z-aligned obstacles to the scene."""
     if kind == "tabletop":
-        env = tabletop_scene(seed, z_offset)
+        env = tabletop_scene(seed, z_offset, n_zaligned=n_zaligned)
     elif kind == "shelf":
-        env = shelf_scene(seed, z_offset)
+        env = shelf_scene(seed, z_offset, n_zaligned=n_zaligned)
     elif kind == "mixed":
-        env = mixed_scene(seed, n_obstacles if n_obstacles is not None else 20)
+        env = mixed_scene(seed, n_obstacles if n_obstacles is not None else 20, n_zaligned=n_zaligned)
     else:
         raise ValueError(kind)
     rng = Rng(seed ^ 0x5A5A5A5A)

@@ -1,3 +1,4 @@
+import os
 import sys
 from pathlib import Path
 
@@ -8,7 +9,19 @@ ROOT = Path(__file__).resolve().parents[1]
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "oracle"))
 GOLDEN = ROOT / "tests" / "golden"
-REFERENCE = Path("/root/reference")
+
+
+def _reference() -> Path:
+    """The pRRTC checkout: $PRRTC_REFERENCE, else the one the oracle's
+    reference builds were made from (recorded by the build), else none."""
+    env = os.environ.get("PRRTC_REFERENCE")
+    if env:
+        return Path(env)
+    rec = ROOT / "oracle" / "_ref" / "REFERENCE"
+    return Path(rec.read_text().strip()) if rec.exists() else ROOT / "oracle" / "_ref" / "no-reference"
+
+
+REFERENCE = _reference()
 
 
 def pytest_configure(config):

@@ -1,8 +1,9 @@
 """Generate the golden fixtures in this directory from the reference itself.
 
-Run in a checkout where pRRTC is available (default /root/reference):
+Run where a pRRTC checkout is available (its path as the argument, else
+$PRRTC_REFERENCE):
 
-    make -C oracle ref          # pRRTC's own checker, compiled from its sources
+    make -C oracle ref REF=/path/to/pRRTC   # pRRTC's own checker, from its sources
     python tests/golden/make_golden.py [/path/to/pRRTC]
 
 For each robot and scene it writes checker_<robot>_<scene>.npz with
@@ -16,6 +17,7 @@ For each robot and scene it writes checker_<robot>_<scene>.npz with
 """
 from __future__ import annotations
 
+import os
 import sys
 from pathlib import Path
 
@@ -30,7 +32,10 @@ from prrtc_gb300.robots import extract, refparse  # noqa: E402
 from pyoracle import OracleLib, RefLib  # noqa: E402
 
 CASES = [("sphere", "tabletop", 11), ("panda", "tabletop", 0), ("panda", "shelf", 1), ("fetch", "mixed", 2),
-         ("baxter", "tabletop", 3), ("baxter", "shelf", 4)]
+         ("baxter", "tabletop", 3), ("baxter", "shelf", 4),
+         # scenes holding z-aligned capsules and z-aligned cuboids as well
+         ("sphere", "zmixed", 12), ("panda", "ztabletop", 5), ("panda", "zshelf", 6), ("fetch", "zmixed", 7),
+         ("baxter", "zmixed", 8)]
 N_UNIFORM, N_SEGMENT, N_FK = 3072, 1024, 64
 
 
@@ -45,17 +50,32 @@ def configs(robot: str, seed: int) -> np.ndarray:
 
 
 def scene(robot, kind, seed):
+    """The fixture's obstacles.  A 'z' prefix adds z-aligned obstacles
+    (vertical capsules, yawed boxes): 20 for the sphere robot, 12 in mixed
+    clutter, 8 on a table, 6 in shelf cells."""
+    nz = 0
+    if kind.startswith("z"):
+        kind = kind[1:]
+        nz = {"mixed": 12, "tabletop": 8, "shelf": 6}[kind]
     if robot == "sphere":
-        return scenes.mixed_scene(seed, 40, lo=(-4, -4, -4), hi=(4, 4, 4))
+        return scenes.mixed_scene(seed, 40, lo=(-4, -4, -4), hi=(4, 4, 4), n_zaligned=20 if nz else 0)
     if kind == "mixed":
-        return scenes.mixed_scene(seed, 40)
-    return scenes.make_query(robot, kind, seed).env if robot != "baxter" else (
-        scenes.tabletop_scene(seed, z_offset=0.3) if kind == "tabletop" else scenes.shelf_scene(seed, z_offset=0.3))
+        return scenes.mixed_scene(seed, 40, n_zaligned=nz)
+    z = 0.3 if robot == "baxter" else 0.0
+    if kind == "tabletop":
+        return scenes.tabletop_scene(seed, z_offset=z, n_zaligned=nz)
+    if robot == "baxter":
+        return scenes.shelf_scene(seed, z_offset=z, n_zaligned=nz)
+    return scenes.make_query(robot, kind, seed, n_zaligned=nz).env
 
 
-def main(ref_root: str):
+def main(ref_root: str, force: bool = False):
+    """Write every fixture that is missing (all of them with force)."""
     O, R = OracleLib(), RefLib()
     for robot, kind, seed in CASES:
+        out = ROOT / "tests" / "golden" / f"checker_{robot}_{kind}.npz"
+        if out.exists() and not force:
+            continue
         env = scene(robot, kind, seed)
         q = configs(robot, seed)
         free_ref = R.check(robot, env, q)
@@ -71,7 +91,6 @@ def main(ref_root: str):
             keys, _ = extract._sphere_keys(prog)
             fk_c = extract._centres(prog, keys, fk_q.astype(np.float64))   # (S, N, 3) in the model's sphere order
             assert fk_c.shape[0] == len(m["spheres"])
-        out = ROOT / "tests" / "golden" / f"checker_{robot}_{kind}.npz"
         np.savez_compressed(out, env_spheres=env.spheres, env_capsules=env.capsules,
                             env_z_capsules=env.z_aligned_capsules, env_cuboids=env.cuboids,
                             env_z_cuboids=env.z_aligned_cuboids, q=q, free_ref=free_ref, margin=margin,
@@ -81,4 +100,7 @@ def main(ref_root: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if a != "--force"]
+    if not args and not os.environ.get("PRRTC_REFERENCE"):
+        sys.exit("usage: make_golden.py [--force] /path/to/pRRTC   (or set PRRTC_REFERENCE)")
+    main(args[0] if args else os.environ["PRRTC_REFERENCE"], force="--force" in sys.argv)

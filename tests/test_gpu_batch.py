@@ -98,14 +98,43 @@ def test_batch_time_budget_and_iteration_limit(ctx):
 
 def test_batch_attempts_and_restarts(ctx, oracle):
     """Extra attempts (idle warps in the tail) and restarts (an attempt that
-    exhausts its arena) keep every returned path valid and solve as many.
-    With 256-node arenas the solved count depends on which warps' extensions
-    land first: over repeated runs it spans about 11 to 21 of 24."""
+    exhausts its arena) keep every returned path valid.  With ample arenas
+    every query is solved; with 256-node arenas attempts run out of nodes, so
+    the run must show restarts (extra attempts), and how many queries end
+    solved depends on which warps' extensions land first (about 11 to 21 of
+    24 over repeated runs): that count is printed, not bounded."""
     from prrtc_gb300 import BatchSettings
     qs = queries("panda", "shelf", 24, 300)
     base = c0(granularity=64, balance=2, tree_ratio=1.0, dynamic_domain=True, range=0.5)
-    for kw in (dict(max_attempts=1), dict(max_attempts=8, restart_after_ns=100000, max_workers_per_attempt=4),
-               dict(max_attempts=8, max_nodes_per_tree=256, restart_after_ns=100000)):
+    for kw in (dict(max_attempts=1), dict(max_attempts=8, restart_after_ns=100000, max_workers_per_attempt=4)):
         res = ctx.solve_batch("panda", qs, BatchSettings(base, **kw))
-        solved = check_all(oracle, "panda", qs, res, 64, need_all=False)
-        assert solved >= (24 if kw.get("max_nodes_per_tree") is None else 8), kw
+        assert check_all(oracle, "panda", qs, res, 64) == 24, kw
+    b = ctx.batch("panda", qs, BatchSettings(base, max_attempts=8, max_nodes_per_tree=256, restart_after_ns=100000))
+    b.run()
+    st = b.stats()
+    solved = check_all(oracle, "panda", qs, b.results(), 64, need_all=False)
+    print(f"256-node arenas: {solved}/24 solved, {st['extra_attempts']} extra attempts")
+    assert st["extra_attempts"] > 0 and st["error"] == 0
+    b.free()
+
+
+def test_batch_idle_wait_limit_ends_run_with_error(ctx, oracle):
+    """A warp that finds no work polls for some; past idle_wait_limit polls it
+    gives up, sets the batch's error flag and returns, so no wait is endless.
+    One hard query with one worker per attempt leaves every other warp idle;
+    with a limit of 64 polls they give up at once.  The run reports
+    PRRTC_ECUDA with stats.error = 1, the working warp still finishes its
+    query (a returned path revalidates), and the context plans normally
+    afterwards."""
+    from prrtc_gb300 import BatchSettings, PrrtcError
+    qs = queries("panda", "shelf", 1, 700)
+    b = ctx.batch("panda", qs, BatchSettings(c0(granularity=64, balance=2, tree_ratio=1.0, dynamic_domain=True),
+                                              max_attempts=1, max_workers_per_attempt=1, idle_wait_limit=64,
+                                              time_budget_ns=int(2e9)))
+    with pytest.raises(PrrtcError):
+        b.run()
+    assert b.stats()["error"] == 1
+    check_all(oracle, "panda", qs, b.results(), 64, need_all=False)
+    b.free()
+    res = ctx.solve_batch("panda", queries("panda", "tabletop", 8, 900), BatchSettings(c0()))
+    assert all(r.solved for r in res)

@@ -24,22 +24,61 @@ def test_checker_matches_reference_golden(case, ctx, oracle):
     assert np.all(z["margin"][bad] < NEAR)
 
 
-SCENES = [("panda", "tabletop", 0), ("panda", "shelf", 1), ("fetch", "mixed", 2), ("baxter", "shelf", 3)]
+SCENES = [("panda", "tabletop", 0), ("panda", "shelf", 1), ("fetch", "mixed", 2), ("baxter", "shelf", 3),
+          ("baxter", "mixed", 4)]
+
+
+def scene(robot, kind, seed):
+    """Every scene also holds z-aligned capsules and z-aligned cuboids
+    (tabletop 8, shelf 6, mixed 12), so all five primitive tests run."""
+    from prrtc_gb300 import scenes
+    if kind == "mixed":
+        return scenes.mixed_scene(seed, 60, n_zaligned=12)
+    if kind == "shelf":
+        return scenes.shelf_scene(seed, 0.3 if robot == "baxter" else 0.0, n_zaligned=6)
+    return scenes.tabletop_scene(seed, n_zaligned=8)
+
+
+def million(robot, seed):
+    from prrtc_gb300 import scenes
+    sc, off = (np.array(v) for v in scenes.LIMITS[robot])
+    rng = np.random.default_rng(100 + seed)
+    return (rng.random((1_000_000, len(sc))) * sc + off).astype(np.float32)
 
 
 @pytest.mark.parametrize("robot,kind,seed", SCENES)
 def test_checker_million_configs(robot, kind, seed, ctx, oracle):
-    from prrtc_gb300 import scenes
-    env = scenes.mixed_scene(seed, 60) if kind == "mixed" else (
-        scenes.shelf_scene(seed, 0.3 if robot == "baxter" else 0.0) if kind == "shelf" else scenes.tabletop_scene(seed))
-    sc, off = (np.array(v) for v in scenes.LIMITS[robot])
-    rng = np.random.default_rng(100 + seed)
-    q = (rng.random((1_000_000, len(sc))) * sc + off).astype(np.float32)
+    env = scene(robot, kind, seed)
+    q = million(robot, seed)
     got = ctx.validate_configs(robot, env, q)
     ref, margin = oracle.check(robot, env, q, margin=True)
     bad = np.flatnonzero(got != ref)
     near = int((margin < NEAR).sum())
     print(f"{robot}/{kind}: 1e6 configs, free {ref.mean():.3f}, mismatches {len(bad)}, near-contact bucket {near}")
+    assert np.all(margin[bad] < NEAR)
+
+
+@pytest.mark.parametrize("robot,kind,seed", SCENES + [("sphere", "mixed", 5)])
+def test_checker_matches_reference_gpu_checker(robot, kind, seed, ctx, oracle):
+    """Verdicts against pRRTC's own GPU checker (fkcc<Robot>, utils.cuh:326-327,
+    compiled for sm_103a from the reference sources into oracle/_ref and
+    loaded as a cubin) on 10^6 seeded configurations per robot, in scenes
+    with every primitive type.  Disagreements may only lie in the
+    near-contact bucket (float64 margin < 1e-5 m), which is counted."""
+    from pyoracle import RefGpuChecker
+    if not RefGpuChecker.available(robot):
+        pytest.skip("reference GPU checker not built (needs a pRRTC checkout at build time)")
+    from prrtc_gb300 import scenes
+    env = scene(robot, kind, seed) if robot != "sphere" else scenes.mixed_scene(
+        seed, 60, (-4, -4, -4), (4, 4, 4), n_zaligned=20)
+    q = million(robot, seed)
+    ref = RefGpuChecker(robot).check(env, q)
+    got = ctx.validate_configs(robot, env, q)
+    _, margin = oracle.check(robot, env, q, margin=True)
+    bad = np.flatnonzero(got != ref)
+    near = int((margin < NEAR).sum())
+    print(f"{robot}/{kind} vs pRRTC GPU checker: 1e6 configs, free {ref.mean():.4f}, mismatches {len(bad)}, "
+          f"near-contact bucket {near}")
     assert np.all(margin[bad] < NEAR)
 
 
@@ -60,8 +99,7 @@ def test_fk_spheres_match_fp64(case, ctx, oracle):
 @pytest.mark.parametrize("g", [1, 32, 128])
 def test_edges_match_oracle(robot, kind, seed, g, ctx, oracle):
     from prrtc_gb300 import scenes
-    env = scenes.mixed_scene(seed, 60) if kind == "mixed" else (
-        scenes.shelf_scene(seed) if kind == "shelf" else scenes.tabletop_scene(seed))
+    env = scene(robot, kind, seed)
     sc, off = (np.array(v) for v in scenes.LIMITS[robot])
     rng = np.random.default_rng(7 + seed)
     a = (rng.random((3000, len(sc))) * sc + off).astype(np.float32)
@@ -129,9 +167,12 @@ def test_maximum_environment_and_zero_length_edges(ctx, oracle):
         return rng.uniform([0.3, -0.8, 0.0], [1.3, 0.8, 1.4], (n, 3))
 
     sph = np.column_stack([pos(256), rng.uniform(0.01, 0.04, 256)]).astype(np.float32)          # 1024 floats
-    caps = np.array([capsule_row(p, p + rng.uniform(-0.1, 0.1, 3), rng.uniform(0.01, 0.03)) for p in pos(256)])  # 2048
-    cubs = np.array([cuboid_row(p, rng.uniform(0.01, 0.05, 3), rng.uniform(-1, 1, 3)) for p in pos(512)])       # 8192
-    env = Environment(spheres=sph, capsules=caps, cuboids=cubs)
+    caps = np.array([capsule_row(p, p + rng.uniform(-0.1, 0.1, 3), rng.uniform(0.01, 0.03)) for p in pos(128)])  # 1024
+    zcaps = np.array([capsule_row(p, p + [0, 0, rng.uniform(0.05, 0.2)], rng.uniform(0.01, 0.03))
+                      for p in pos(128)])                                                          # 1024
+    cubs = np.array([cuboid_row(p, rng.uniform(0.01, 0.05, 3), rng.uniform(-1, 1, 3)) for p in pos(256)])       # 4096
+    zcubs = np.array([cuboid_row(p, rng.uniform(0.01, 0.05, 3), (0, 0, rng.uniform(-3, 3))) for p in pos(256)])  # 4096
+    env = Environment(spheres=sph, capsules=caps, z_aligned_capsules=zcaps, cuboids=cubs, z_aligned_cuboids=zcubs)
     assert env.packed_floats() == 11264
     q = scenes._uniform_configs("panda", scenes.Rng(9), 20000).astype(np.float32)
     got = ctx.validate_configs("panda", env, q)

@@ -27,13 +27,38 @@ def test_oracle_matches_reference_live(robot, oracle):
         build(ref=True)
     R = RefLib()
     from prrtc_gb300 import scenes
-    env = scenes.mixed_scene(99, 60) if robot != "sphere" else scenes.mixed_scene(99, 60, (-4, -4, -4), (4, 4, 4))
+    env = scenes.mixed_scene(99, 60, n_zaligned=12) if robot != "sphere" else scenes.mixed_scene(
+        99, 60, (-4, -4, -4), (4, 4, 4), n_zaligned=20)
     sc, off = (np.array(v) for v in scenes.LIMITS[robot])
     q = (np.random.default_rng(3).random((100000, len(sc))) * sc + off).astype(np.float32)
     a = R.check(robot, env, q)
     b, m = oracle.check(robot, env, q, margin=True)
     bad = np.flatnonzero(a != b)
     assert np.all(m[bad] < 1e-5)
+
+
+@pytest.mark.parametrize("robot", ["sphere", "panda", "fetch", "baxter"])
+def test_zaligned_fixtures_decide_verdicts(robot, oracle):
+    """Each robot has a golden fixture holding z-aligned capsules and
+    z-aligned cuboids whose verdicts depend on them: dropping either type
+    frees some configurations (utils.cuh:134-148,178-197 really run)."""
+    from prrtc_gb300.env import Environment
+    flips_c = flips_b = 0
+    for case in golden_cases():
+        if not case.startswith(robot + "_z"):
+            continue
+        env, z = load_golden(case)
+        assert len(env.z_aligned_capsules) and len(env.z_aligned_cuboids)
+        q = z["q"]
+        full = oracle.check(robot, env, q)
+        np.testing.assert_array_equal(full[z["margin"] > 1e-5], z["free_ref"][z["margin"] > 1e-5])
+        no_c = Environment(spheres=env.spheres, capsules=env.capsules, cuboids=env.cuboids,
+                           z_aligned_cuboids=env.z_aligned_cuboids)
+        no_b = Environment(spheres=env.spheres, capsules=env.capsules, cuboids=env.cuboids,
+                           z_aligned_capsules=env.z_aligned_capsules)
+        flips_c += int((oracle.check(robot, no_c, q) != full).sum())
+        flips_b += int((oracle.check(robot, no_b, q) != full).sum())
+    assert flips_c > 0 and flips_b > 0, (flips_c, flips_b)
 
 
 MBM = [("panda", REFERENCE / "scripts/panda_problems.json"), ("fetch", REFERENCE / "scripts/fetch_problems.json")]

@@ -44,6 +44,51 @@ def test_noalloc_matches_validate_configs_two_calls():
     ctx.close()
 
 
+def test_noalloc_queued_calls_on_one_stream_and_empty_scene():
+    """Two calls queued back to back on one non-default stream, with a single
+    synchronise after both (the second reuses the fixed array while the first
+    may still be running, ordered by the stream), then a call with no
+    obstacles at all.  Each verdict buffer matches prrtc_validate_configs,
+    and the first also matches the oracle outside the near-contact bucket."""
+    import sys
+    import torch
+    import prrtc_gb300.build as b
+    b.build()
+    from conftest import ROOT
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from pyoracle import OracleLib
+    from prrtc_gb300 import Context, api, scenes
+    from prrtc_gb300.env import Environment
+    f = _noalloc()
+    ctx = Context(0)
+    envs = [scenes.tabletop_scene(7, n_zaligned=8), scenes.shelf_scene(8, n_zaligned=6), Environment()]
+    sc, off = (np.array(v) for v in scenes.LIMITS["panda"])
+    qs = [(np.random.default_rng(20 + i).random((30000, 7)) * sc + off).astype(np.float32) for i in range(3)]
+    st = torch.cuda.Stream()
+    outs, keep = [], []
+    with torch.cuda.stream(st):
+        qd = [torch.from_numpy(q).cuda() for q in qs]
+        for i in range(2):
+            out = torch.full((len(qs[i]),), 7, dtype=torch.uint8, device="cuda")
+            d, k = api._env_desc(envs[i])
+            keep.append((d, k))
+            assert f(api.robot_id("panda"), C.byref(d), qd[i].data_ptr(), len(qs[i]), out.data_ptr(),
+                     C.c_void_p(st.cuda_stream)) == 0
+            outs.append(out)
+    st.synchronize()
+    d, k = api._env_desc(envs[2])
+    out = torch.full((len(qs[2]),), 7, dtype=torch.uint8, device="cuda")
+    assert f(api.robot_id("panda"), C.byref(d), qd[2].data_ptr(), len(qs[2]), out.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    outs.append(out)
+    for env, q, o in zip(envs, qs, outs):
+        np.testing.assert_array_equal(o.cpu().numpy(), ctx.validate_configs("panda", env, q))
+    ref, margin = OracleLib().check("panda", envs[0], qs[0], margin=True)
+    bad = np.flatnonzero(outs[0].cpu().numpy() != ref)
+    assert (margin[bad] < 1e-5).all()
+    ctx.close()
+
+
 def test_noalloc_rejects_environment_beyond_the_fixed_array():
     import torch
     from prrtc_gb300 import api
