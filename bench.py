@@ -50,8 +50,6 @@ from prrtc_gb300.workloads import SETTINGS as WORKLOAD_SETTINGS  # noqa: E402
 MARGIN = 1e-5   # planning margin (m): every returned path clears contact by 10 micrometres
 GPU_BUDGET_NS = int(30e9)   # per batch launch; unsolved queries past it count as failures
 CPU_BUDGET_S = 20.0         # per query in the CPU restatement
-PLAIN_BUDGET_S = 30.0       # total for the plain-form comparison
-PLAIN_QUERIES = 128         # the plain form's sample of the first step's queries
 
 
 def log(*a):
@@ -194,6 +192,33 @@ def reduce_over_ranks(t_dev: float, solved: int, world: int, device: str = "cpu"
     return t, int(c)
 
 
+def bulk_and_tail(results):
+    """The launch's bulk rate and its tail.  bulk: solved queries that
+    finished by the 99th-percentile finish time, over that time (device
+    clock from the launch's start), so one hard query's solve time does not
+    set it.  tail: the query that ended the launch (solve and finish times,
+    samples drawn, tree sizes, status), and every unsolved query's status,
+    samples and tree sizes."""
+    fin = np.array([r.finish_ns for r in results if r.solved], np.float64)
+    if not len(fin):
+        return None, None
+    t99 = float(np.percentile(fin, 99))
+    bulk = {"queries_per_s": float((fin <= t99).sum()) / (t99 * 1e-9), "p99_finish_ms": t99 / 1e6,
+            "last_finish_ms": float(fin.max()) / 1e6}
+    last = max(range(len(results)), key=lambda i: results[i].finish_ns)
+    r = results[last]
+
+    def desc(i, r):
+        return {"query": i, "solved": bool(r.solved), "status": int(r.status), "solve_ms": r.kernel_ns / 1e6,
+                "finish_ms": r.finish_ns / 1e6, "samples": int(r.samples), "start_tree_size": r.start_tree_size,
+                "goal_tree_size": r.goal_tree_size}
+
+    unsolved = [desc(i, x) for i, x in enumerate(results) if not x.solved]
+    tail = {"last": desc(last, r), "unsolved": unsolved[:16], "unsolved_count": len(unsolved),
+            "status_legend": "0 sample budget (max_iters x num_new_configs) spent, 2 arena full, 3 time budget"}
+    return bulk, tail
+
+
 def h2d_bytes(qs):
     b = 0
     for q in qs:
@@ -247,9 +272,16 @@ def ours(args, rank, world):
     results = stream.results()
     solved = sum(r.solved for r in results)
     t_dev = st["kernel_ns"] * 1e-9
+    bulk, tail = bulk_and_tail(results)
     t_dev, solved = reduce_over_ranks(t_dev, solved, world, f"cuda:{dev}")
     value = solved / t_dev
     lat = [r.kernel_ns / 1e6 for r in results if r.solved]
+    if args.kernel_only:
+        # a profiling run: the planner launches above and nothing else
+        if rank == 0:
+            print(json.dumps({"kernel_only": True, "queries": len(qs), "solved": solved, "ms": t_dev * 1e3,
+                              "flops": st["flops"], "bulk_ms": st["bulk_ns"] / 1e6}), flush=True)
+        return
 
     # ---- e2e through the C ABI with host buffers (same streamed job): the
     # prrtc_query array points at host start, goal and obstacle arrays, as a C
@@ -283,31 +315,22 @@ def ours(args, rank, world):
     bad = sum(1 for q, r in zip(qs, results)
               if r.solved and not O.check_edges(robot, q.env, r.path[:-1], r.path[1:], g).all())
 
-    # ---- the plain single-query form on the first step's queries, one at a time
-    plain_t, plain_solved, plain_ms = 0.0, 0, []
-    ctx.set_planning_margin(MARGIN)
-    ctx.set_time_budget(int(GPU_BUDGET_NS))
-    for q, e in zip(first[:PLAIN_QUERIES], envs[:PLAIN_QUERIES]):
-        r = ctx.solve(robot, q.start, q.goal, e, plan)
-        plain_t += r.wall_ns * 1e-9
-        plain_solved += r.solved
-        plain_ms.append(r.wall_ns / 1e6)
-        if plain_t > PLAIN_BUDGET_S:
-            break
-    ns_plain = len(plain_ms)
-    plain_qps = plain_solved / plain_t
+    # ---- distributional comparison on the first DIST_QUERIES queries of the
+    # timed run: batched (this run's results), plain (the drop-in) and the
+    # oracle's rrtc on the host cores; the plain and CPU figures below are
+    # this leg's
+    dist = {args.workload: distribution_leg(ctx, O, args.workload, qs, envs, batched=results)}
+    plain_row = dist[args.workload]["plain_gpu"]
+    plain_qps = plain_row["queries_per_s"]
+    cpu_row = dist[args.workload]["oracle_cpu"]
 
     # ---- roofline: FP32 work of the planner kernel vs the measured FP32 peak
     peak = ctx.measure_fp32_peak()
     achieved = st["flops"] / (st["kernel_ns"] * 1e-9) / 1e12
     nn_bytes = st["nn_nodes"] * 4 * plan_dof(robot)
 
-    # ---- CPU baseline (bounded sample)
-    ns_cpu = min(cpu_sample_size(args.workload), len(qs))
-    threads = os.cpu_count() or 1
-    cs, cdt, _ = cpu_planner(robot, qs[:ns_cpu], plan, threads)
-
-    # ---- the other configurations, one launch each
+    # ---- the other configurations, one launch each; the tabletop one also
+    # gets the distributional comparison (its first DIST_QUERIES queries)
     others, baxter = {}, None
     if args.others:
         for name, cnt in OTHER_WORKLOADS:
@@ -317,7 +340,13 @@ def ours(args, rank, world):
             others[f"{name}_{cnt}"] = info
             if name == "baxter_mixed":
                 baxter = run
+            if name == "panda_tabletop":
+                oq, ores, oenvs = run
+                dist[name] = distribution_leg(ctx, O, name, oq, oenvs, batched=ores)
             log(name, json.dumps(info))
+
+    # ---- the stand-alone checker (validator) on the C0 and C1 scenes
+    validator = validator_leg(ctx, peak) if args.validator else None
 
     # ---- differentiable clearance: smoothing of this run's paths (and Baxter's)
     clearance = None
@@ -339,9 +368,15 @@ def ours(args, rank, world):
         "one_batch": {"queries": n, "ms_median": single_med, "ms_all": single_ms,
                       "queries_per_s": statistics.median(single_solved) / (single_med * 1e-3),
                       "note": "the first step's queries alone in one launch: its time is its slowest query's"},
-        "plain": {"queries_per_s": plain_qps, "p50_solve_ms": statistics.median(plain_ms),
-                  "max_solve_ms": max(plain_ms), "sample": f"{ns_plain} of the first step's {n} queries",
-                  "solved": plain_solved, "batched_over_plain": value / plain_qps},
+        "bulk": bulk,
+        "tail": tail,
+        "plain": {"queries_per_s": plain_qps, "p50_solve_ms": plain_row["p50_solve_ms"],
+                  "success_rate": plain_row["success_rate"],
+                  "sample": f"the first {DIST_QUERIES} queries of the timed run, one at a time",
+                  "batched_over_plain": value / plain_qps if plain_qps else None,
+                  "batched_bulk_over_plain": bulk["queries_per_s"] / plain_qps if bulk and plain_qps else None},
+        "distribution": dist,
+        "validator": validator,
         "e2e": {"value": e2e_solved / e2e_t, "unit": "queries/s", "h2d_bytes_per_step": int(h2d) // args.steps,
                 "d2h_bytes_per_step": int(d2h) // args.steps, "call_ms": e2e_t * 1e3,
                 "create_ms": res_e2e[0].copy_ns / 1e6 if res_e2e else None},
@@ -352,15 +387,91 @@ def ours(args, rank, world):
                      "traffic": (lambda b: b * len(qs) if b else None)(profiled_dram_bytes_per_query(args.workload)),
                      "traffic_source": "ncu capture of 256 queries (profiles/), scaled by queries processed",
                      "peak_source": "measured FP32 FMA chain kernel on this GPU (prrtc_measure_fp32_peak)",
-                     "nn_scan_bytes_per_s": nn_bytes / (st["kernel_ns"] * 1e-9)},
-        "cpu_baseline": {"value": cs / cdt, "unit": "queries/s", "cores": threads, "kind": "port",
-                         "sample": f"first {ns_cpu} of the {len(qs)} queries, oracle RRT-Connect restatement"},
+                     "nn_scan_bytes_per_s": nn_bytes / (st["kernel_ns"] * 1e-9),
+                     "bulk": ({"achieved": st["bulk_flops"] / (st["bulk_ns"] * 1e-9) / 1e12,
+                               "frac": st["bulk_flops"] / (st["bulk_ns"] * 1e-9) / 1e12 / peak,
+                               "ms": st["bulk_ns"] / 1e6,
+                               "note": "the launch up to the moment 99 % of its queries had finished"}
+                              if st["bulk_ns"] else None)},
+        "cpu_baseline": {"value": cpu_row["queries_per_s"], "unit": "queries/s", "cores": cpu_row["threads"],
+                         "kind": "port",
+                         "sample": f"the first {DIST_QUERIES} of the {len(qs)} queries, oracle RRT-Connect "
+                                   f"restatement, {DIST_CPU_BUDGET_S:.0f} s per query"},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "other_workloads": others or None,
         "clearance": clearance,
     }
     print(json.dumps(line), flush=True)
+
+
+DIST_QUERIES = 256          # seeds per configuration in the distributional comparison
+DIST_CPU_BUDGET_S = 10.0    # per query, the oracle's rrtc on the host cores
+DIST_PLAIN_BUDGET_NS = int(5e9)   # per query, the plain form
+
+
+def quantiles(costs):
+    if not len(costs):
+        return None
+    c = np.asarray(costs, np.float64)
+    return {"p10": float(np.percentile(c, 10)), "p50": float(np.percentile(c, 50)), "p90": float(np.percentile(c, 90))}
+
+
+def distribution_leg(ctx, O, name, qs, envs, batched=None):
+    """Success rate and path-cost quantiles over the same DIST_QUERIES seeded
+    queries for three planners: the GPU batched form, the GPU plain form (the
+    drop-in, one query at a time, with pRRTC's own lane count) and the
+    oracle's restatement of pRRTC's rrtc on the host cores (the reference
+    algorithm; OpenMP over queries, DIST_CPU_BUDGET_S per query).  Cost is
+    pRRTC's: the summed length of the traced edges (pRRTC.cu:561,571).
+    `batched`: results of these queries from a run already made, else one
+    batch launch here."""
+    from prrtc_gb300 import BatchSettings, autotune, workloads
+    robot = workloads.WORKLOADS[name][0]
+    plan = settings_for(name)
+    qs, envs = qs[:DIST_QUERIES], envs[:DIST_QUERIES]
+    n = len(qs)
+    if batched is None:
+        batched = ctx.solve_batch(robot, [(e, q.start, q.goal) for e, q in zip(envs, qs)],
+                                  BatchSettings(plan, use_graph=0, margin=MARGIN, time_budget_ns=GPU_BUDGET_NS,
+                                                **autotune.load(robot, name)), path_capacity=2048)
+    batched = batched[:n]
+    ctx.set_planning_margin(MARGIN)
+    ctx.set_time_budget(DIST_PLAIN_BUDGET_NS)
+    plain, plain_t = [], 0.0
+    for q, e in zip(qs, envs):
+        r = ctx.solve(robot, q.start, q.goal, e, plan)
+        plain.append(r)
+        plain_t += r.wall_ns * 1e-9
+    g = plan.granularity
+    plain_bad = sum(1 for q, r in zip(qs, plain)
+                    if r.solved and not O.check_edges(robot, q.env, r.path[:-1], r.path[1:], g).all())
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    ores, _ = O.solve_many(robot, np.stack([q.start for q in qs]), np.stack([q.goal for q in qs]),
+                           [q.env for q in qs], plan, threads=threads, path_cap=16, budget_s=DIST_CPU_BUDGET_S)
+    cpu_t = time.perf_counter() - t0
+
+    def row(res, extra=None):
+        solved = [r for r in res if r.solved]
+        d = {"success_rate": len(solved) / n, "cost": quantiles([r.cost for r in solved])}
+        d.update(extra or {})
+        return d
+
+    lat = [r.wall_ns / 1e6 for r in plain if r.solved]
+    out = {"queries": n, "settings": WORKLOAD_SETTINGS[name],
+           "batched_gpu": row(batched),
+           "plain_gpu": row(plain, {"queries_per_s": sum(r.solved for r in plain) / plain_t,
+                                    "p50_solve_ms": statistics.median(lat) if lat else None,
+                                    "revalidated": f"{sum(r.solved for r in plain) - plain_bad}/"
+                                                   f"{sum(r.solved for r in plain)}",
+                                    "budget_s": DIST_PLAIN_BUDGET_NS * 1e-9}),
+           "oracle_cpu": row(ores, {"queries_per_s": sum(r.solved for r in ores) / cpu_t, "threads": threads,
+                                    "budget_s": DIST_CPU_BUDGET_S, "wall_s": cpu_t}),
+           "note": "batched: margin 1e-5 m, tuned lanes; plain: pRRTC's settings and lane count, margin 1e-5 m; "
+                   "oracle: pRRTC's rrtc restated (lanes round-robin), margin 0"}
+    log("distribution", name, json.dumps(out))
+    return out
 
 
 def smooth_and_judge(ctx, O, robot, envs, hosts, P):
@@ -422,20 +533,19 @@ OTHER_BUDGET_NS = int(10e9)   # per launch of the other configurations
 
 
 def workload_run(ctx, O, name, n):
-    """One batched launch of workload `name` (after one warm-up launch): solved
-    queries/s over the launch, solve-time percentiles, edge validations/s,
-    every path revalidated by the oracle.  A launch whose unsolved queries run
-    into the time budget lasts the budget, so the span up to the last solved
-    query is reported beside it."""
+    """One batched launch of workload `name` (after a warm-up launch of its
+    first 32 queries): solved queries/s over the launch, the bulk rate and
+    tail (bulk_and_tail), solve-time percentiles, edge validations/s, every
+    path revalidated by the oracle.  A launch whose unsolved queries run into
+    the time budget lasts the budget; the tail says which queries and why."""
     from prrtc_gb300 import BatchSettings, autotune, workloads
     robot = workloads.WORKLOADS[name][0]
     qs = workloads.make(name, n)
     envs = [ctx.upload_env(q.env) for q in qs]
     plan = settings_for(name)
-    b = ctx.batch(robot, [(e, q.start, q.goal) for e, q in zip(envs, qs)],
-                  BatchSettings(plan, use_graph=1, margin=MARGIN, time_budget_ns=OTHER_BUDGET_NS,
-                                **autotune.load(robot, name)), path_capacity=2048)
-    b.run()
+    bs = BatchSettings(plan, use_graph=1, margin=MARGIN, time_budget_ns=OTHER_BUDGET_NS, **autotune.load(robot, name))
+    ctx.solve_batch(robot, [(e, q.start, q.goal) for e, q in zip(envs[:32], qs[:32])], bs)
+    b = ctx.batch(robot, [(e, q.start, q.goal) for e, q in zip(envs, qs)], bs, path_capacity=2048)
     b.run()
     st, res = b.stats(), b.results()
     b.free()
@@ -444,12 +554,10 @@ def workload_run(ctx, O, name, n):
     g = plan.granularity
     bad = sum(1 for q, r in zip(qs, res) if r.solved and not O.check_edges(robot, q.env, r.path[:-1], r.path[1:], g).all())
     lat = [r.kernel_ns / 1e6 for r in res if r.solved]
-    span = max(lat) * 1e-3 if lat else None
+    bulk, tail = bulk_and_tail(res)
     info = {"queries": n, "settings": WORKLOAD_SETTINGS[name], "queries_per_s": solved / t, "ms": t * 1e3,
             "success_rate": solved / n, "revalidated": f"{solved - bad}/{solved}",
-            "budget_s": OTHER_BUDGET_NS * 1e-9, "unsolved_in_budget": n - solved,
-            "solved_span_ms": span * 1e3 if span else None,
-            "queries_per_s_over_solved_span": solved / span if span else None,
+            "budget_s": OTHER_BUDGET_NS * 1e-9, "unsolved_in_budget": n - solved, "bulk": bulk, "tail": tail,
             "p50_solve_ms": statistics.median(lat) if lat else None,
             "p90_solve_ms": float(np.percentile(lat, 90)) if lat else None,
             "p99_solve_ms": float(np.percentile(lat, 99)) if lat else None,
@@ -457,6 +565,64 @@ def workload_run(ctx, O, name, n):
             "configs_per_s": st["configs_checked"] / t,
             "fp32_tflops": st["flops"] / t / 1e12}
     return info, (qs, res, envs)
+
+
+VALIDATOR_SCENES = [("C0 panda tabletop (seed 0)", "tabletop", 0, 32), ("C1 panda shelf (seed 1)", "shelf", 1, 128)]
+VALIDATOR_N = 1 << 20
+VALIDATOR_EDGES = 1 << 14
+VALIDATOR_REPS = 5
+
+
+def validator_leg(ctx, peak):
+    """The stand-alone checker (prrtc_validate_configs / prrtc_validate_edges)
+    on the C0 and C1 scenes: 2^20 configurations, uniformly random and
+    collision-free, and 2^14 edges between collision-free configurations at
+    the scene's granularity.  Inputs are resident on the device; each launch
+    is timed with CUDA events on the library's stream (prrtc_last_kernel_ns),
+    a 256 MB write flushes L2 before each, and the median of 5 is reported.
+    FLOPs are the checker's counted algorithmic work (the reference
+    hierarchy's executed tests x weights + canonical FK)."""
+    import torch
+    from prrtc_gb300 import scenes
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    out = {"peak_tflops": peak, "configs": VALIDATOR_N, "edges": VALIDATOR_EDGES, "reps": VALIDATOR_REPS}
+
+    def timed(fn):
+        ms, fl = [], []
+        for _ in range(VALIDATOR_REPS):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            ctx.work_counters(reset=True)
+            fn()
+            ms.append(ctx.last_kernel_ns() / 1e6)
+            fl.append(ctx.work_counters(reset=True)[0])
+        k = int(np.argsort(ms)[len(ms) // 2])
+        return ms[k], fl[k]
+
+    for label, kind, seed, g in VALIDATOR_SCENES:
+        env = scenes.make_query("panda", kind, seed).env
+        e = ctx.upload_env(env)
+        rnd = scenes._uniform_configs("panda", scenes.Rng(4242 + seed), VALIDATOR_N)
+        q = torch.from_numpy(rnd).cuda()
+        free = ctx.validate_configs("panda", e, q).cpu().numpy().astype(bool)
+        fq = rnd[free]
+        fq = np.resize(fq, (VALIDATOR_N, 7)) if len(fq) else rnd
+        qf = torch.from_numpy(np.ascontiguousarray(fq)).cuda()
+        rows = {}
+        for name, qq in (("random", q), ("collision_free", qf)):
+            ms, fl = timed(lambda: ctx.validate_configs("panda", e, qq))
+            rows[name] = {"ms": ms, "configs_per_s": VALIDATOR_N / (ms * 1e-3),
+                          "tflops": fl / (ms * 1e-3) / 1e12, "frac": fl / (ms * 1e-3) / 1e12 / peak}
+        rows["random"]["free_fraction"] = float(free.mean())
+        a = torch.from_numpy(np.ascontiguousarray(fq[:VALIDATOR_EDGES])).cuda()
+        b = torch.from_numpy(np.ascontiguousarray(np.roll(fq, 1, axis=0)[:VALIDATOR_EDGES])).cuda()
+        ms, fl = timed(lambda: ctx.validate_edges("panda", e, a, b, g))
+        rows["edges"] = {"granularity": g, "ms": ms, "edge_validations_per_s": VALIDATOR_EDGES / (ms * 1e-3),
+                         "configs_per_s": VALIDATOR_EDGES * g / (ms * 1e-3), "tflops": fl / (ms * 1e-3) / 1e12,
+                         "frac": fl / (ms * 1e-3) / 1e12 / peak}
+        out[label] = rows
+        log("validator", label, json.dumps(rows))
+    return out
 
 
 def profiled_dram_bytes_per_query(workload: str):
@@ -484,10 +650,13 @@ def main():
     ap.add_argument("--queries", type=int, default=1024)
     ap.add_argument("--no-clearance", dest="clearance", action="store_false",
                     help="skip the path-smoothing measurement")
-    ap.add_argument("--others", action="store_true",
-                    help="also run the other configurations (Panda tabletop, Fetch, Baxter) one launch each; "
-                         "they are parity cases, not the benchmark, and Baxter's launches run to a 10 s budget")
-    ap.add_argument("--no-others", dest="others", action="store_false", help=argparse.SUPPRESS)
+    ap.add_argument("--no-others", dest="others", action="store_false",
+                    help="skip the other configurations (Panda tabletop, Fetch, Baxter: one launch each, "
+                         "parity cases beside the benchmark)")
+    ap.add_argument("--no-validator", dest="validator", action="store_false",
+                    help="skip the stand-alone checker measurement")
+    ap.add_argument("--kernel-only", action="store_true",
+                    help="run the warm-up and timed planner launches only and print a short line (for profilers)")
     args = ap.parse_args()
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
         # started without a launcher: one rank per GPU on this node

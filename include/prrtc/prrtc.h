@@ -125,6 +125,9 @@ typedef struct prrtc_result {
     uint64_t wall_ns;        /* whole call, host clock */
     uint64_t kernel_ns;      /* planner kernel(s), device clock */
     uint64_t copy_ns;        /* host<->device copies of the query */
+    uint64_t finish_ns;      /* batched form: from the launch's start to this query's end
+                                (device clock; 0 if it never started) */
+    int64_t samples;         /* batched form: samples drawn for this query, all attempts */
 } prrtc_result;
 
 /* ---- context ------------------------------------------------------------ */
@@ -209,6 +212,10 @@ prrtc_status prrtc_sample_goals(prrtc_ctx *ctx, prrtc_robot robot, const prrtc_e
 prrtc_status prrtc_fk_spheres(prrtc_ctx *ctx, prrtc_robot robot, const float *q, int64_t n,
                               float *out);
 
+/* Device time of the context's last prrtc_validate_configs or
+ * prrtc_validate_edges launch (CUDA events on the context's stream around the
+ * kernel alone), in ns.  No counterpart in the reference. */
+prrtc_status prrtc_last_kernel_ns(prrtc_ctx *ctx, uint64_t *ns);
 /* Work counters: algorithmic FLOPs (weights as prrtc_batch_stats.flops) and
  * configurations checked by validate_configs / validate_edges / solve since
  * the last reset. */
@@ -275,6 +282,8 @@ typedef struct prrtc_batch_settings {
     uint32_t idle_wait_limit;        /* polls (about 256 ns each) a warp with no work to take makes
                                         before it gives up and the run ends with PRRTC_ECUDA and
                                         stats.error = 1 (0: 2^22, about a second) */
+    int shared_frames;               /* 1: the checker keeps its forward-kinematics frames in each
+                                        warp's shared memory; 0: in local memory (cached by L1) */
 } prrtc_batch_settings;
 
 typedef struct prrtc_batch prrtc_batch;
@@ -294,6 +303,10 @@ typedef struct prrtc_batch_stats {
                                         tests executed x {sphere 11, capsule 26, z-capsule 16,
                                         cuboid 27, z-cuboid 18, sphere pair 11} */
     uint64_t nn_nodes;               /* tree nodes visited by nearest-neighbour scans */
+    uint64_t bulk_ns;                /* device time from the launch's start until 99 % of the queries
+                                        had finished (the launch without its tail) */
+    uint64_t bulk_flops;             /* flops counted by then */
+    uint64_t bulk_configs;           /* configurations checked by then */
 } prrtc_batch_stats;
 
 void prrtc_batch_settings_default(prrtc_batch_settings *s);

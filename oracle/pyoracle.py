@@ -339,12 +339,13 @@ class RefGpuChecker(_Cubin):
 
 class RefSampler(_Cubin):
     """pRRTC's own sampler (oracle/ref_planner_gpu.cu, which includes
-    pRRTC.cu unmodified; `make -C oracle ref_sampler`): the reference's
-    init_rng kernel (pRRTC.cu:107-111, seed 1 as pRRTC::solve passes it),
-    then halton_initialize / halton_next / scale_cfg for every lane."""
+    pRRTC.cu unmodified; `make -C oracle ref_sampler`): cuRAND states as
+    pRRTC's init_rng makes them (pRRTC.cu:107-111, seed 1 as pRRTC::solve
+    passes it), then the reference's halton_initialize / halton_next /
+    scale_cfg for every lane."""
 
     PATH = HERE / "_ref" / "ref_sampler.cubin"
-    INIT_RNG = "_ZN6pRRTC8init_rngEP17curandStateXORWOWmi"   # pRRTC::init_rng(curandState*, unsigned long, int)
+    INIT_RNG = "ref_init_rng"
 
     def __init__(self):
         super().__init__(self.PATH, [self.INIT_RNG, "ref_curand_state_bytes"] +
@@ -374,3 +375,151 @@ class RefSampler(_Cubin):
                      C.c_void_p(cfg.data_ptr()), C.c_int(lanes), C.c_int(steps)])
         torch.cuda.synchronize()
         return bases.cpu().numpy(), raw.cpu().numpy(), cfg.cpu().numpy()
+
+
+class RefPlanner(_Cubin):
+    """pRRTC's own planner kernel rrtc<Robot> (pRRTC.cu:305-602, in the cubin
+    `make -C oracle ref_sampler` builds), driven the way pRRTC::solve drives
+    it (pRRTC.cu:607-747): settings into d_settings, trees of -9999 nodes,
+    cuRAND and Halton states, the start and goal roots, one launch of
+    num_new_configs blocks of `granularity` threads, then the solved flag,
+    tree sizes, cost and the two path halves read back and assembled goal
+    first.
+
+    That kernel writes tree slots past max_samples before it gives up
+    (pRRTC.cu:451-453,535-537) and traces paths into a fixed
+    path[2][5000] (pRRTC.cu:559-572) without bounds checks, so it runs here
+    only under settings for which every write provably stays in bounds
+    (`safe_rows` raises otherwise):
+      * dynamic domain off, so every iteration of a block that does not
+        return appends (no unbounded skip loop), and a block runs at most
+        max_iters + 1 iterations (pRRTC.cu:343-346, 598);
+      * an iteration appends at most 1 + E nodes to its block's tree, E =
+        ceil(joint-box diameter / range) extension steps (every node lies in
+        the box, so no connect distance exceeds its diameter);
+      * so a tree holds at most R = roots + B (max_iters + 1) (1 + E) nodes,
+        B = num_new_configs; the trees are allocated with R rows (more than
+        max_samples if need be), and the parents arrays are zero-filled, so a
+        parent read before its write lands is a valid index;
+      * a traced half-path has at most R - 1 nodes, and R x dof <= 5000;
+      * granularity a power of two <= 128 (the block's reduction reads
+        sdata[tid + s] for every tid, pRRTC.cu:398-408, inside sdata[256])."""
+
+    RRTC = {"sphere": "6Sphere", "panda": "5Panda", "fetch": "5Fetch", "baxter": "6Baxter"}
+    MAX_PATH = 5000
+    FLT_MAX = 3.4028234663852886e38
+
+    def __init__(self, robot: str):
+        r = self.RRTC[robot]
+        self.k_rrtc = (f"_ZN5pRRTC4rrtcIN4ppln6robots{r}EEEvPPfPPiS5_PNS_11HaltonStateIT_EEP17curandStateXORWOW"
+                       f"PNS1_9collision11EnvironmentIfEE")
+        self.k_halton = f"_ZN5pRRTC11init_haltonIN4ppln6robots{r}EEEvPNS_11HaltonStateIT_EEP17curandStateXORWOW"
+        super().__init__(RefSampler.PATH, [self.k_rrtc, self.k_halton, "ref_init_rng", "ref_reset", "ref_read",
+                                           "ref_env_build", "ref_env_bytes", "ref_curand_state_bytes"])
+        torch = self.torch
+        self.robot = robot
+        self.dim = {"sphere": 3, "panda": 7, "fetch": 8, "baxter": 14}[robot]
+        sz = torch.zeros(5, dtype=torch.int64, device="cuda")
+        self.launch("ref_curand_state_bytes", 1, 1, [C.c_void_p(sz.data_ptr())])
+        es = torch.zeros(5, dtype=torch.int64, device="cuda")
+        self.launch("ref_env_bytes", 1, 1, [C.c_void_p(es.data_ptr())])
+        torch.cuda.synchronize()
+        sz = [int(v) for v in sz.cpu()]
+        self.rng_bytes = sz[0]
+        self.halton_bytes = sz[1 + ["sphere", "panda", "fetch", "baxter"].index(robot)]
+        self.env_sizes = [int(v) for v in es.cpu()]
+        cu = self._driver()
+        cu.cuModuleGetGlobal_v2.restype = C.c_int
+        cu.cuModuleGetGlobal_v2.argtypes = [C.POINTER(C.c_uint64), C.POINTER(C.c_size_t), C.c_void_p, C.c_char_p]
+        cu.cuMemcpyHtoD_v2.restype = C.c_int
+        cu.cuMemcpyHtoD_v2.argtypes = [C.c_uint64, C.c_void_p, C.c_size_t]
+        self.d_settings, nbytes = C.c_uint64(), C.c_size_t()
+        self._ok(cu.cuModuleGetGlobal_v2(C.byref(self.d_settings), C.byref(nbytes), self.mod,
+                                         b"_ZN5pRRTC10d_settingsE"), "d_settings")
+        self.settings_bytes = nbytes.value
+
+    @classmethod
+    def available(cls) -> bool:
+        return RefSampler.PATH.exists()
+
+    @staticmethod
+    def safe_rows(robot: str, settings, num_goals: int) -> int:
+        """Tree rows that hold every node the kernel can append under these
+        settings; raises ValueError when they are not provably safe."""
+        import math
+        from prrtc_gb300 import scenes
+        dim = {"sphere": 3, "panda": 7, "fetch": 8, "baxter": 14}[robot]
+        if settings.dynamic_domain:
+            raise ValueError("dynamic domain: a block may skip iterations without bound")
+        g = settings.granularity
+        if g < 1 or g > 128 or g & (g - 1):
+            raise ValueError("granularity must be a power of two <= 128")
+        diam = math.sqrt(sum(s * s for s in scenes.LIMITS[robot][0])) * (1 + 1e-6)
+        ext = math.ceil(diam / settings.range)
+        rows = max(1, num_goals) + settings.num_new_configs * (settings.max_iters + 1) * (1 + ext)
+        if rows * dim > RefPlanner.MAX_PATH:
+            raise ValueError(f"a traced path could need {rows * dim} floats > {RefPlanner.MAX_PATH}")
+        return max(rows, settings.max_samples)
+
+    def solve(self, start, goals, env, settings) -> dict:
+        torch = self.torch
+        D = self.dim
+        start = _arr(start, D)
+        goals = _arr(goals, D)
+        ng = len(goals)
+        rows = self.safe_rows(self.robot, settings, ng)
+        B, g = settings.num_new_configs, settings.granularity
+        s_bytes = C.string_at(C.addressof(settings), C.sizeof(settings))
+        assert len(s_bytes) == self.settings_bytes == 44
+        self._ok(self._driver().cuMemcpyHtoD_v2(self.d_settings.value, s_bytes, len(s_bytes)), "settings")
+        dev = "cuda"
+        nodes = [torch.full((rows * D,), -9999.0, dtype=torch.float32, device=dev) for _ in range(2)]
+        parents = [torch.zeros(rows, dtype=torch.int32, device=dev) for _ in range(2)]
+        radii = [torch.zeros(rows, dtype=torch.float32, device=dev) for _ in range(2)]
+        radii[0][0] = self.FLT_MAX
+        radii[1][:ng] = self.FLT_MAX
+        nodes[0][:D] = torch.from_numpy(start.reshape(-1)).to(dev)
+        nodes[1][:ng * D] = torch.from_numpy(goals.reshape(-1)).to(dev)
+        parents[1][:ng] = torch.arange(ng, dtype=torch.int32, device=dev)
+        ptrs = [torch.tensor([t[0].data_ptr(), t[1].data_ptr()], dtype=torch.int64, device=dev)
+                for t in (nodes, parents, radii)]
+        nrng = B * D
+        rng = torch.zeros(nrng * self.rng_bytes + 256, dtype=torch.uint8, device=dev)
+        halton = torch.zeros(B * self.halton_bytes + 256, dtype=torch.uint8, device=dev)
+        self.launch("ref_init_rng", (nrng + 63) // 64, 64, [C.c_void_p(rng.data_ptr()), C.c_ulong(1), C.c_int(nrng)])
+        self.launch(self.k_halton, (B + 63) // 64, 64, [C.c_void_p(halton.data_ptr()), C.c_void_p(rng.data_ptr())])
+        self.launch("ref_reset", 1, 1, [C.c_int(1), C.c_int(ng)])
+        arrs = [torch.from_numpy(_arr(a, k)).to(dev) for a, k in
+                ((env.spheres, 4), (env.capsules, 8), (env.z_aligned_capsules, 8), (env.cuboids, 15),
+                 (env.z_aligned_cuboids, 15))]
+        per = [self.env_sizes[1], self.env_sizes[2], self.env_sizes[2], self.env_sizes[3], self.env_sizes[3]]
+        nbytes = (self.env_sizes[0] + 255) // 256 * 256 + sum((p * len(a) + 255) // 256 * 256 for p, a in zip(per, arrs))
+        scratch = torch.zeros(nbytes + 256, dtype=torch.uint8, device=dev)
+        eargs = [C.c_void_p(scratch.data_ptr())]
+        for a in arrs:
+            eargs += [C.c_void_p(a.data_ptr() if len(a) else 0), C.c_int(len(a))]
+        self.launch("ref_env_build", 1, 1, eargs)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        self.launch(self.k_rrtc, B, g, [C.c_void_p(p.data_ptr()) for p in ptrs] +
+                    [C.c_void_p(halton.data_ptr()), C.c_void_p(rng.data_ptr()), C.c_void_p(scratch.data_ptr())])
+        ev1.record()
+        ints = torch.zeros(7, dtype=torch.int32, device=dev)
+        cost = torch.zeros(1, dtype=torch.float32, device=dev)
+        path = torch.zeros(2 * self.MAX_PATH, dtype=torch.float32, device=dev)
+        self.launch("ref_read", 1, 1, [C.c_void_p(ints.data_ptr()), C.c_void_p(cost.data_ptr()),
+                                       C.c_void_p(path.data_ptr())])
+        torch.cuda.synchronize()
+        ii = [int(v) for v in ints.cpu()]
+        out = {"solved": ii[0] == 1, "start_tree_size": ii[1], "goal_tree_size": ii[2], "iters": ii[6],
+               "kernel_ms": ev0.elapsed_time(ev1), "cost": float(cost.item()), "path": None}
+        if out["solved"]:
+            p = path.cpu().numpy().reshape(2, self.MAX_PATH)
+            n0, n1 = ii[3], ii[4]
+            rows_out = [goals[ii[5]]]
+            rows_out += [p[1, i * D:(i + 1) * D] for i in range(n1 - 1, -1, -1)]
+            rows_out += [p[0, i * D:(i + 1) * D] for i in range(n0)]
+            rows_out.append(start[0])
+            out["path"] = np.stack(rows_out).astype(np.float32)
+            out["path_length"] = n0 + n1
+        return out

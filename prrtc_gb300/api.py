@@ -68,7 +68,8 @@ class _Result(C.Structure):
     _fields_ = [("solved", C.c_int), ("status", C.c_int), ("start_tree_size", C.c_int), ("goal_tree_size", C.c_int),
                 ("path_length", C.c_int), ("iters", C.c_int), ("cost", C.c_float), ("path_rows", C.c_int),
                 ("path_capacity", C.c_int), ("path", C.POINTER(C.c_float)), ("wall_ns", C.c_uint64),
-                ("kernel_ns", C.c_uint64), ("copy_ns", C.c_uint64)]
+                ("kernel_ns", C.c_uint64), ("copy_ns", C.c_uint64), ("finish_ns", C.c_uint64),
+                ("samples", C.c_int64)]
 
 
 class _Query(C.Structure):
@@ -85,7 +86,7 @@ class BatchSettings(C.Structure):
                 ("blocks_per_sm", C.c_int),
                 ("use_graph", C.c_int),
                 ("margin", C.c_float), ("time_budget_ns", C.c_uint64), ("admission", C.c_int),
-                ("idle_wait_limit", C.c_uint32)]
+                ("idle_wait_limit", C.c_uint32), ("shared_frames", C.c_int)]
 
     def __init__(self, plan: Settings | None = None, **kw):
         super().__init__()
@@ -112,7 +113,8 @@ class SmoothSettings(C.Structure):
 class _BatchStats(C.Structure):
     _fields_ = [("kernel_ns", C.c_uint64), ("samples", C.c_int64), ("solved", C.c_int), ("blocks", C.c_int),
                 ("warps_per_block", C.c_int), ("slots", C.c_int), ("error", C.c_int), ("extra_attempts", C.c_int),
-                ("configs_checked", C.c_uint64), ("flops", C.c_uint64), ("nn_nodes", C.c_uint64)]
+                ("configs_checked", C.c_uint64), ("flops", C.c_uint64), ("nn_nodes", C.c_uint64),
+                ("bulk_ns", C.c_uint64), ("bulk_flops", C.c_uint64), ("bulk_configs", C.c_uint64)]
 
 
 @dataclass
@@ -129,6 +131,8 @@ class PlannerResult:
     kernel_ns: int = 0
     copy_ns: int = 0
     status: int = 0
+    finish_ns: int = 0       # batched form: launch start to this query's end (device clock)
+    samples: int = 0         # batched form: samples drawn, all attempts
 
 
 def lib():
@@ -160,6 +164,7 @@ def lib():
             "prrtc_solve": (C.c_int, [vp, C.c_int, fp, fp, C.c_int, vp, C.POINTER(Settings), C.POINTER(_Result)]),
             "prrtc_measure_fp32_peak": (C.c_int, [vp, C.POINTER(C.c_double)]),
             "prrtc_work_counters": (C.c_int, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.c_int]),
+            "prrtc_last_kernel_ns": (C.c_int, [vp, C.POINTER(C.c_uint64)]),
             "prrtc_batch_settings_default": (None, [C.POINTER(BatchSettings)]),
             "prrtc_batch_create": (C.c_int, [vp, C.c_int, C.POINTER(_Query), C.c_int, C.POINTER(BatchSettings), C.POINTER(vp)]),
             "prrtc_batch_run": (C.c_int, [vp, vp]),
@@ -264,6 +269,12 @@ class Context:
         f, n = C.c_uint64(), C.c_uint64()
         self._check(lib().prrtc_work_counters(self.handle, C.byref(f), C.byref(n), int(reset)))
         return f.value, n.value
+
+    def last_kernel_ns(self) -> int:
+        """Device time of the last validate_configs / validate_edges kernel."""
+        v = C.c_uint64()
+        self._check(lib().prrtc_last_kernel_ns(self.handle, C.byref(v)))
+        return v.value
 
     def set_planning_margin(self, pad: float):
         self._check(lib().prrtc_set_planning_margin(self.handle, pad))
@@ -492,10 +503,12 @@ class PreparedBatch:
     def results(self) -> list:
         res, paths = self.res, self.paths
         cols = {f: res[f].tolist() for f in ("solved", "path_rows", "start_tree_size", "goal_tree_size", "path_length",
-                                             "iters", "cost", "wall_ns", "kernel_ns", "copy_ns", "status")}
+                                             "iters", "cost", "wall_ns", "kernel_ns", "copy_ns", "status", "finish_ns",
+                                             "samples")}
         return [PlannerResult(bool(cols["solved"][i]), paths[i, :cols["path_rows"][i]].copy(), cols["start_tree_size"][i],
                               cols["goal_tree_size"][i], cols["path_length"][i], cols["iters"][i], cols["cost"][i],
-                              cols["wall_ns"][i], cols["kernel_ns"][i], cols["copy_ns"][i], cols["status"][i])
+                              cols["wall_ns"][i], cols["kernel_ns"][i], cols["copy_ns"][i], cols["status"][i],
+                              cols["finish_ns"][i], cols["samples"][i])
                 for i in range(len(res))]
 
 
@@ -542,7 +555,8 @@ class Batch:
             res[i].path = paths[i].ctypes.data_as(C.POINTER(C.c_float))
         self.ctx._check(lib().prrtc_batch_results(self.ctx.handle, self.handle, res))
         return [PlannerResult(bool(r.solved), paths[i, :r.path_rows].copy(), r.start_tree_size, r.goal_tree_size,
-                              r.path_length, r.iters, r.cost, r.wall_ns, r.kernel_ns, r.copy_ns, r.status)
+                              r.path_length, r.iters, r.cost, r.wall_ns, r.kernel_ns, r.copy_ns, r.status, r.finish_ns,
+                              r.samples)
                 for i, r in enumerate(res)]
 
     def stats(self) -> dict:

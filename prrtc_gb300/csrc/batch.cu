@@ -111,6 +111,7 @@ struct prrtc_batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // last run
     prrtc_batch_stats stats{};
+    unsigned long long t0 = 0;     // device clock at the last run's start (first warp)
     bool ran = false;
 };
 
@@ -278,6 +279,7 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     P.bases_lanes = c->bases_lanes;
     P.restart_after_ns = settings->restart_after_ns ? settings->restart_after_ns : 10000000ull;
     P.idle_limit = settings->idle_wait_limit ? settings->idle_wait_limit : (1u << 22);
+    P.shared_frames = settings->shared_frames ? 1 : 0;
     // pRRTC stops a query when any of its num_new_configs lanes passes max_iters
     // (pRRTC.cu:343-346), i.e. after about max_iters x num_new_configs samples
     // below 2^31 with room for the tickets that warps take after the last one
@@ -296,7 +298,7 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     P.halton_bases = c->bases;
     prrtc_robot_limits(robot, P.scale, P.offset);
     // launch shape
-    const int occ = ops->batch_occupancy(b->wpb, P.env_records);
+    const int occ = ops->batch_occupancy(b->wpb, P.env_records, P.shared_frames);
     int per_sm = settings->blocks_per_sm > 0 ? std::min(settings->blocks_per_sm, std::max(occ, 1)) : std::max(occ, 1);
     b->blocks = c->sms * per_sm;
     b->stats.blocks = b->blocks;
@@ -354,10 +356,14 @@ extern "C" prrtc_status prrtc_batch_run(prrtc_ctx *ctx, prrtc_batch *b)
     cudaEventElapsedTime(&ms, b->ev0, b->ev1);
     b->stats.kernel_ns = (uint64_t)(ms * 1e6);
     b->stats.error = ctr.error;
+    b->t0 = ctr.t0;
     b->stats.configs_checked = ctr.work[1];
     b->stats.extra_attempts = ctr.attempts;
     b->stats.flops = ctr.work[0];
     b->stats.nn_nodes = ctr.nn_nodes;
+    b->stats.bulk_ns = ctr.t99 > ctr.t0 ? ctr.t99 - ctr.t0 : 0;
+    b->stats.bulk_flops = ctr.work99[0];
+    b->stats.bulk_configs = ctr.work99[1];
     b->ran = true;
     // every slot must be free again, i.e. its arena region back to NaN
     std::vector<SlotState> sl(b->slots);
@@ -410,6 +416,8 @@ extern "C" prrtc_status prrtc_batch_results(prrtc_ctx *ctx, prrtc_batch *b, prrt
         r.iters = o.solved ? o.iters : -1;
         r.cost = o.cost;
         r.kernel_ns = o.t_done > o.t_admit ? o.t_done - o.t_admit : 0;
+        r.finish_ns = (o.t_done > b->t0 && b->t0) ? o.t_done - b->t0 : 0;
+        r.samples = o.samples;
         r.wall_ns = b->stats.kernel_ns;
         r.copy_ns = 0;
         r.path_rows = 0;

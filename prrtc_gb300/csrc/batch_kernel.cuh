@@ -42,10 +42,13 @@ struct alignas(16) WarpScratch {
     int bad;
 };
 
-template <int D>
-__host__ __device__ constexpr size_t warp_scratch_bytes(int env_records)
+// A warp's shared memory: its WarpScratch, then room for env_records
+// obstacle records, then (with shared frames) the checker's frame area.
+template <class Gen>
+__host__ __device__ constexpr size_t warp_scratch_bytes(int env_records, bool shared_frames)
 {
-    return sizeof(WarpScratch<D>) + (size_t)env_records * sizeof(float4);
+    return sizeof(WarpScratch<Gen::kDof>) + (size_t)env_records * sizeof(float4) +
+           (shared_frames ? shared_frame_bytes(Gen::kFrames) : 0);
 }
 
 // Exact early rejection of dynamic-domain samples.  When every lane of a
@@ -192,8 +195,8 @@ __device__ __forceinline__ bool sample_group(const BatchParams &P, const WarpScr
 // gives round r the points 32 r + lane + 1; interleaved order gives it
 // lane * R + r + 1, so the first round already samples the whole edge at
 // stride R.  Adds the work done to work[0] (FLOPs) and work[1] (points).
-template <class Gen>
-__device__ __forceinline__ bool warp_validate(const WarpScratch<Gen::kDof> &W, int g, int interleave, CheckCtx &ctx,
+template <class Gen, class Ctx>
+__device__ __forceinline__ bool warp_validate(const WarpScratch<Gen::kDof> &W, int g, int interleave, Ctx &ctx,
                                               unsigned long long *work)
 {
     constexpr int D = Gen::kDof;
@@ -232,6 +235,19 @@ __device__ __forceinline__ bool warp_validate(const WarpScratch<Gen::kDof> &W, i
 
 __device__ __forceinline__ int vload(const int *p) { return *(const volatile int *)p; }
 
+// lane 0: count a finished query.  The one that completes 99 % of the batch
+// records the time and the work counters at that moment, so the host can
+// report the launch's bulk apart from its tail.
+__device__ __forceinline__ void count_done(const BatchParams &P, unsigned long long t)
+{
+    const int k = atomicAdd(&P.ctr->done, 1) + 1;
+    if (k == (P.num_queries * 99 + 99) / 100) {
+        P.ctr->t99 = t;
+        P.ctr->work99[0] = *(volatile unsigned long long *)&P.ctr->work[0];
+        P.ctr->work99[1] = *(volatile unsigned long long *)&P.ctr->work[1];
+    }
+}
+
 // lane 0: publish an unsolved query's result (first caller wins)
 __device__ __forceinline__ void finish_query_unsolved(const BatchParams &P, const SlotState *S, int q, int status)
 {
@@ -249,7 +265,7 @@ __device__ __forceinline__ void finish_query_unsolved(const BatchParams &P, cons
     o.samples = vs->ticket;
     o.t_done = global_ns();
     __threadfence();
-    atomicAdd(&P.ctr->done, 1);
+    count_done(P, o.t_done);
 }
 
 // lane 0: end the attempt in slot S unsolved (first caller wins).  The last
@@ -359,7 +375,7 @@ __device__ void batch_trace(const BatchParams &P, const SlotState *S, int s, int
     }
     out.t_done = global_ns();
     __threadfence();
-    atomicAdd(&P.ctr->done, 1);
+    count_done(P, out.t_done);
 }
 
 // whole warp: write query qa's roots into slot s as attempt `attempt` and start it
@@ -508,9 +524,11 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
     constexpr int D = Gen::kDof;
     constexpr unsigned FULL = 0xffffffffu;
     extern __shared__ float4 s_raw[];
-    char *const warp_smem = reinterpret_cast<char *>(s_raw) + (threadIdx.x >> 5) * warp_scratch_bytes<D>(P.env_records);
+    char *const warp_smem =
+        reinterpret_cast<char *>(s_raw) + (threadIdx.x >> 5) * warp_scratch_bytes<Gen>(P.env_records, P.shared_frames);
     WarpScratch<D> &W = *reinterpret_cast<WarpScratch<D> *>(warp_smem);
     float4 *const W_env = reinterpret_cast<float4 *>(warp_smem + sizeof(WarpScratch<D>));
+    float4 *const W_frames = W_env + P.env_records;   // the checker's frames (shared_frames)
     const int lane = lane_id();
     BatchCounters *C = P.ctr;
     const float fg = (float)P.granularity;
@@ -694,6 +712,12 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
             envp = W_env;
         }
         CheckCtx ctx{{envp, Qd.env_n}, P.pad, &W.bad};
+        SharedCheckCtx sctx{ctx, W_frames + lane};
+        // every point of an edge through the robot's checker, frames where P says
+        auto validate = [&]() {
+            return P.shared_frames ? warp_validate<Gen>(W, P.granularity, P.edge_order, sctx, C->work)
+                                   : warp_validate<Gen>(W, P.granularity, P.edge_order, ctx, C->work);
+        };
         float *nodes_s = P.nodes + (size_t)slot * 2 * D * P.cap;
         int *par_s = P.parents + (size_t)slot * 2 * P.cap;
         float *rad_s = P.radii + (size_t)slot * 2 * P.cap;
@@ -852,7 +876,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                         W.step[lane] = __fdiv_rn(__fsub_rn(c, nn), fg);
                     }
                     __syncwarp();
-                    if (!warp_validate<Gen>(W, P.granularity, P.edge_order, ctx, C->work)) {
+                    if (!validate()) {
                         if (lane == 0 && P.dynamic_domain)
                             dd_shrink(rd_t + ni, P.dd_alpha, P.dd_radius, P.dd_min_radius);
                         continue;
@@ -899,7 +923,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                             W.step[lane] = __fdiv_rn(__fsub_rn(b, a), fg);
                         }
                         __syncwarp();
-                        if (!warp_validate<Gen>(W, P.granularity, P.edge_order, ctx, C->work)) break;
+                        if (!validate()) break;
                         int idx2 = -1;
                         if (lane == 0) {
                             idx2 = atomicAdd(&S->free_index[tj], 1);

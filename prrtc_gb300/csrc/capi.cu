@@ -167,7 +167,8 @@ prrtc_status prrtc_create(prrtc_ctx **out, int device)
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
         cudaMalloc(&c->work_dev, 2 * sizeof(unsigned long long)) != cudaSuccess ||
-        cudaMemset(c->work_dev, 0, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+        cudaMemset(c->work_dev, 0, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaEventCreate(&c->kev[0]) != cudaSuccess || cudaEventCreate(&c->kev[1]) != cudaSuccess) {
         cudaGetLastError();
         delete c;
         return PRRTC_ECUDA;
@@ -190,9 +191,20 @@ prrtc_status prrtc_destroy(prrtc_ctx *ctx)
         release_arena(c);
         release_clearance_state(c);
         cudaFree(c->work_dev);
+        for (cudaEvent_t ev : c->kev)
+            if (ev) cudaEventDestroy(ev);
         cudaStreamDestroy(c->stream);
     }
     delete c;
+    return PRRTC_OK;
+}
+
+prrtc_status prrtc_last_kernel_ns(prrtc_ctx *ctx, uint64_t *ns)
+{
+    Ctx *c = Ctx::of(ctx);
+    if (!c || !ns) return PRRTC_EINVAL;
+    std::lock_guard<std::mutex> g(c->mu);
+    *ns = c->last_kernel_ns;
     return PRRTC_OK;
 }
 
@@ -317,10 +329,14 @@ prrtc_status prrtc_validate_configs(prrtc_ctx *ctx, prrtc_robot robot, const prr
     if ((s = c->device_view(q, sizeof(float) * ops->dof * n, 0, true, &dq))) return s;
     if ((s = c->device_view(out_free, n, 1, false, &dout))) return s;
     LaunchEnv le{e->dev, e->counts, c->sms, c->work_dev};
+    cudaEventRecord(c->kev[0], c->stream);
     if ((s = c->cuda(ops->validate_configs(le, (const float *)dq, n, (uint8_t *)dout, c->stream), "validate_configs launch"))) return s;
+    cudaEventRecord(c->kev[1], c->stream);
     c->launches++;
     if (dout != out_free && (s = c->cuda(cudaMemcpyAsync(out_free, dout, n, cudaMemcpyDeviceToHost, c->stream), "copy out"))) return s;
-    return c->cuda(cudaStreamSynchronize(c->stream), "validate_configs");
+    if ((s = c->cuda(cudaStreamSynchronize(c->stream), "validate_configs"))) return s;
+    c->note_kernel_time();
+    return PRRTC_OK;
 }
 
 prrtc_status prrtc_sample_goals(prrtc_ctx *ctx, prrtc_robot robot, const prrtc_env *env, int sphere,
@@ -384,12 +400,16 @@ prrtc_status prrtc_validate_edges(prrtc_ctx *ctx, prrtc_robot robot, const prrtc
     if ((s = c->device_view(b, cb, 2, true, &db))) return s;
     if ((s = c->device_view(out_free, n, 1, false, &dout))) return s;
     LaunchEnv le{e->dev, e->counts, c->sms, c->work_dev};
+    cudaEventRecord(c->kev[0], c->stream);
     if ((s = c->cuda(ops->validate_edges(le, (const float *)da, (const float *)db, n, granularity, (uint8_t *)dout, c->stream),
                      "validate_edges launch")))
         return s;
+    cudaEventRecord(c->kev[1], c->stream);
     c->launches++;
     if (dout != out_free && (s = c->cuda(cudaMemcpyAsync(out_free, dout, n, cudaMemcpyDeviceToHost, c->stream), "copy out"))) return s;
-    return c->cuda(cudaStreamSynchronize(c->stream), "validate_edges");
+    if ((s = c->cuda(cudaStreamSynchronize(c->stream), "validate_edges"))) return s;
+    c->note_kernel_time();
+    return PRRTC_OK;
 }
 
 prrtc_status prrtc_fk_spheres(prrtc_ctx *ctx, prrtc_robot robot, const float *q, int64_t n, float *out)

@@ -76,6 +76,8 @@ struct Ctx {
     float plan_pad = 0.0f;                  // prrtc_set_planning_margin
     unsigned long long budget_ns = 0;       // prrtc_set_time_budget
     ClearanceState *clearance = nullptr;    // robot tables for the clearance cost
+    cudaEvent_t kev[2] = {nullptr, nullptr};   // around the last checker launch (prrtc_last_kernel_ns)
+    uint64_t last_kernel_ns = 0;
 
     static Ctx *of(prrtc_ctx *c) { return reinterpret_cast<Ctx *>(c); }
     prrtc_status fail(prrtc_status s, const char *fmt, ...);
@@ -84,6 +86,13 @@ struct Ctx {
     void *scratch(int slot, size_t bytes);
     prrtc_status device_view(const void *p, size_t bytes, int slot, bool in, void **out);
     void release_planner_state();
+    // after a synchronised checker launch bracketed by kev: its device time
+    void note_kernel_time()
+    {
+        float ms = 0.0f;
+        last_kernel_ns = cudaEventElapsedTime(&ms, kev[0], kev[1]) == cudaSuccess ? (uint64_t)(ms * 1e6) : 0;
+        cudaGetLastError();
+    }
 };
 
 const RobotOps *robot_ops(prrtc_robot r);

@@ -242,12 +242,59 @@ __device__ __forceinline__ Frame relative_frame(const Frame &A, const Frame &B)
     return R;
 }
 
+// Where a table-form checker keeps its frames (F[0] the world, F[q + 1] the
+// frame of joint q) while it walks the schedule.
+//
+// LocalFrames: an array per thread.  The schedule indexes it with table
+// values, so it lives in local memory, cached by L1 while it fits there.
+//
+// SharedFrames: one column per lane in a warp's shared-memory area, float4
+// k (0..2) of frame i (i >= 1) at p[(3 (i - 1) + k) * 32], p = area + lane.
+// A warp's 32 lanes touch 32 consecutive float4 per access (no bank
+// conflicts), every read hits, and nothing competes with it for L1.  The
+// world frame is not stored.  shared_frame_bytes(N) is a warp's area.
+template <int N>
+struct LocalFrames {
+    Frame F[N];
+    __device__ __forceinline__ void set(int i, const Frame &f) { F[i] = f; }
+    __device__ __forceinline__ const Frame *view() const { return F; }
+};
+
+struct SharedFrames {
+    float4 *p;
+    __device__ __forceinline__ void set(int i, const Frame &f)
+    {
+        if (i == 0) return;
+        float4 *q = p + 3 * (i - 1) * 32;
+        q[0] = make_float4(f.m[0], f.m[1], f.m[2], f.m[3]);
+        q[32] = make_float4(f.m[4], f.m[5], f.m[6], f.m[7]);
+        q[64] = make_float4(f.m[8], f.m[9], f.m[10], f.m[11]);
+    }
+    __device__ __forceinline__ SharedFrames view() const { return *this; }
+};
+
+__host__ __device__ constexpr size_t shared_frame_bytes(int frames)
+{
+    return (size_t)(frames > 1 ? frames - 1 : 0) * 3 * 32 * sizeof(float4);
+}
+
+__device__ __forceinline__ Frame frame_at(const Frame *F, int i) { return F[i]; }
+
+__device__ __forceinline__ Frame frame_at(const SharedFrames F, int i)
+{
+    if (i == 0) return Frame{{1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f}};
+    const float4 *q = F.p + 3 * (i - 1) * 32;
+    const float4 a = q[0], b = q[32], c = q[64];
+    return Frame{{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w}};
+}
+
 // What the generated checkers call.  pad = 0 and stop_flag = nullptr give the
 // reference checker's verdicts; planners may inflate every sphere by pad
 // (a certified margin) and share a flag through which any lane's collision
 // ends the other lanes' work on the same edge.  `work` accumulates the
 // algorithmic FLOPs of the primitive tests executed (reference weights).
 struct CheckCtx {
+    static constexpr bool kSharedFrames = false;   // table-form frames in a local array
     EnvView env;
     float pad;
     volatile int *stop_flag;
@@ -278,9 +325,27 @@ struct CheckCtx {
     __device__ __forceinline__ bool stop() const { return stop_flag != nullptr && *stop_flag != 0; }
 };
 
+// The same checks with the table-form frames in the warp's shared-memory
+// area (frames: the area's base + lane, see SharedFrames).
+struct SharedCheckCtx : CheckCtx {
+    static constexpr bool kSharedFrames = true;
+    float4 *frames;
+};
+
+// The frame store a generated checker uses with context type Ctx.
+template <class Ctx, int N, bool = Ctx::kSharedFrames>
+struct FrameStore : LocalFrames<N> {
+    __device__ __forceinline__ explicit FrameStore(const Ctx &) {}
+};
+template <class Ctx, int N>
+struct FrameStore<Ctx, N, true> : SharedFrames {
+    __device__ __forceinline__ explicit FrameStore(const Ctx &c) : SharedFrames{c.frames} {}
+};
+
 // The schedule of a table-form checker (see GenSched); returns true when free.
-template <class Ctx>
-__device__ __noinline__ bool run_schedule(const Frame *F, const GenSched *__restrict__ sched, int nsched,
+// F is a frame view: a local array (const Frame *) or SharedFrames.
+template <class Frames, class Ctx>
+__device__ __noinline__ bool run_schedule(const Frames F, const GenSched *__restrict__ sched, int nsched,
                                           const GenEnvGroup *__restrict__ eg, const GenLeafBlock *__restrict__ lb,
                                           const float4 *__restrict__ leaves, const GenSelfGroup *__restrict__ sg,
                                           const GenPairBlock *__restrict__ pb, const LeafPair *__restrict__ pairs,
@@ -293,23 +358,24 @@ __device__ __noinline__ bool run_schedule(const Frame *F, const GenSched *__rest
             bool go = true;
             if (g.has_gate) {
                 float x, y, z;
-                xform(F[g.gate_frame + 1], g.gate, x, y, z);
+                xform(frame_at(F, g.gate_frame + 1), g.gate, x, y, z);
                 go = ctx.env_hit(x, y, z, g.gate.w);
             }
             if (go)
                 for (int k = g.first_block; k < g.first_block + g.nblocks; k++) {
                     const GenLeafBlock b = lb[k];
-                    if (ctx.env_leaves(F[b.frame + 1], leaves + b.first, b.n)) return false;
+                    if (ctx.env_leaves(frame_at(F, b.frame + 1), leaves + b.first, b.n)) return false;
                 }
         } else {
             const GenSelfGroup g = sg[e.index];
             float ax, ay, az, bx, by, bz;
-            xform(F[g.fa + 1], g.a, ax, ay, az);
-            xform(F[g.fb + 1], g.b, bx, by, bz);
+            xform(frame_at(F, g.fa + 1), g.a, ax, ay, az);
+            xform(frame_at(F, g.fb + 1), g.b, bx, by, bz);
             if (ctx.pair_hit(ax - bx, ay - by, az - bz, g.a.w + g.b.w))
                 for (int k = g.first_block; k < g.first_block + g.nblocks; k++) {
                     const GenPairBlock b = pb[k];
-                    if (ctx.self_pairs(relative_frame(F[b.fa + 1], F[b.fb + 1]), pairs + b.first, b.n)) return false;
+                    if (ctx.self_pairs(relative_frame(frame_at(F, b.fa + 1), frame_at(F, b.fb + 1)), pairs + b.first, b.n))
+                        return false;
                 }
         }
         if (ctx.stop()) return true;

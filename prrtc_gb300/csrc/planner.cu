@@ -289,6 +289,8 @@ extern "C" prrtc_status prrtc_solve(prrtc_ctx *ctx, prrtc_robot robot, const flo
     copy_ns += ns_since(copy1);
     res->kernel_ns = (uint64_t)(kms * 1e6);
     res->copy_ns = copy_ns;
+    res->finish_ns = res->kernel_ns;
+    res->samples = 0;
     res->wall_ns = ns_since(wall0);
     return (prrtc_status)res->status;
 }

@@ -116,6 +116,8 @@ struct BatchCounters {
     unsigned long long t0;
     unsigned long long work[2];      // algorithmic FLOPs of the checks, configurations checked
     unsigned long long nn_nodes;     // tree nodes visited by nearest-neighbour scans
+    unsigned long long t99;          // device clock when 99 % of the queries had finished
+    unsigned long long work99[2];    // work[] at that moment
 };
 
 // cap on a batch query's samples: 2^31 - 2^24, so that tickets taken past it
@@ -145,6 +147,7 @@ struct BatchParams {
     int bases_lanes;     // rows of halton_bases
     unsigned long long restart_after_ns;   // a query may get its k-th extra attempt after k x this
     unsigned idle_limit;                   // polls before an idle warp gives up (error flag)
+    int shared_frames;                     // the checker's frames in the warp's shared memory (else local)
     const float *cfg_pool;
     const BatchQueryDesc *queries;
     const int *order;    // admission order (query ids), null: index order
@@ -210,7 +213,7 @@ struct RobotOps {
     cudaError_t (*fk_spheres)(const float *q, int64_t n, float *out, int sms, cudaStream_t);
     cudaError_t (*solve_plain)(const PlainParams &, int threads, cudaStream_t);
     cudaError_t (*solve_batch)(const BatchParams &, int blocks, int warps_per_block, cudaStream_t);
-    int (*batch_occupancy)(int warps_per_block, int env_records);   // resident blocks per SM
+    int (*batch_occupancy)(int warps_per_block, int env_records, int shared_frames);   // resident blocks per SM
     cudaError_t (*smooth_paths)(const ClrLaunch &, size_t env_bytes, cudaStream_t);
     cudaError_t (*goal_flags)(const LaunchEnv &, const GoalQuery &, uint8_t *flags, cudaStream_t);
 };

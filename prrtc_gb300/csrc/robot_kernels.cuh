@@ -402,14 +402,22 @@ struct RobotKernels {
     }
     static cudaError_t solve_batch(const BatchParams &P, int blocks, int wpb, cudaStream_t st)
     {
-        const size_t smem = warp_scratch_bytes<Gen::kDof>(P.env_records) * wpb;
+        // (batch_occupancy, called when the batch is created, set the kernel's
+        // dynamic shared-memory limit for this size)
+        const size_t smem = warp_scratch_bytes<Gen>(P.env_records, P.shared_frames) * wpb;
         k_rrtc_batch<Gen><<<blocks, 32 * wpb, smem, st>>>(P);
         return cudaGetLastError();
     }
-    static int batch_occupancy(int wpb, int env_records)
+    static int batch_occupancy(int wpb, int env_records, int shared_frames)
     {
         int n = 0;
-        const size_t smem = warp_scratch_bytes<Gen::kDof>(env_records) * wpb;
+        const size_t smem = warp_scratch_bytes<Gen>(env_records, shared_frames != 0) * wpb;
+        if (smem > 48 * 1024 &&
+            cudaFuncSetAttribute(k_rrtc_batch<Gen>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_rrtc_batch<Gen>, 32 * wpb, smem) != cudaSuccess) {
             cudaGetLastError();
             return 0;
@@ -459,6 +467,7 @@ struct RobotKernels {
     struct NAME {                                                                                   \
         static constexpr int kDof = NS::kDof;                                                       \
         static constexpr int kNumSpheres = NS::kNumSpheres;                                         \
+        static constexpr int kFrames = NS::kFrames;                                                 \
         static constexpr unsigned kFkFlops = NS::kFkFlops;                                          \
         template <class Ctx>                                                                        \
         static __device__ __forceinline__ bool fkcc(const float *q, Ctx &ctx)                       \

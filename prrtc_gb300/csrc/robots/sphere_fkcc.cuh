@@ -8,6 +8,7 @@
 namespace prrtc { namespace gen_sphere {
 
 constexpr int kDof = 3;
+constexpr int kFrames = 4;   // the world and one frame per joint
 constexpr int kNumSpheres = 1;
 constexpr int kNumLeaves = 1;
 constexpr int kNumPairs = 1;

@@ -326,11 +326,11 @@ def emit_cuda_checker(m: dict) -> str:
         # every frame, in chain order, into F[q + 1]; then the schedule loop
         nj = len(m["joints"])
         frames = [fk.frame(jt["q"]) for jt in m["joints"]]
-        code.lines.append(f"Frame F[{nj + 1}];")
-        code.lines.append("F[0] = Frame{{1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f}};")
+        code.lines.append(f"FrameStore<Ctx, {nj + 1}> F(ctx);")
+        code.lines.append("F.set(0, Frame{{1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f}});")
         for jt, T in zip(m["joints"], frames):
-            code.lines.append(f"F[{jt['q'] + 1}] = {_frame_arg(T)};")
-        code.lines.append(f"return run_schedule(F, k{R}Sched, {len(m['schedule'])}, k{R}EnvGroup, k{R}LeafBlock, k{R}Leaf, "
+            code.lines.append(f"F.set({jt['q'] + 1}, {_frame_arg(T)});")
+        code.lines.append(f"return run_schedule(F.view(), k{R}Sched, {len(m['schedule'])}, k{R}EnvGroup, k{R}LeafBlock, k{R}Leaf, "
                           f"k{R}SelfGroup, k{R}PairBlock, k{R}Pair, ctx);")
         tcode = code
         code = _Code()              # the straight-line form, if any, goes to its own code
@@ -390,6 +390,7 @@ def emit_cuda_checker(m: dict) -> str:
     w(f"namespace prrtc {{ namespace gen_{name} {{")
     w("")
     w(f"constexpr int kDof = {m['dof']};")
+    w(f"constexpr int kFrames = {len(m['joints']) + 1};   // the world and one frame per joint")
     w(f"constexpr int kNumSpheres = {len(sp)};")
     w(f"constexpr int kNumLeaves = {max(1, len(leaf_rows))};")
     w(f"constexpr int kNumPairs = {max(1, len(pair_rows))};")

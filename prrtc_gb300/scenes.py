@@ -263,9 +263,14 @@ def _sd_env(env: Environment, p: np.ndarray, r: np.ndarray) -> np.ndarray:
 def clearance(robot: str, env: Environment, q: np.ndarray) -> np.ndarray:
     """Float64 clearance of each configuration: min signed distance over leaf
     spheres vs obstacles and listed leaf self pairs (< 0: penetration)."""
-    m = load_model(robot)
+    return clearance_model(load_model(robot), env, q)
+
+
+def clearance_model(m: dict, env: Environment, q: np.ndarray) -> np.ndarray:
+    """clearance() for a model given as a dict (e.g. one built from a URDF)."""
+    from .robots.extract import model_sphere_centres
     q = np.asarray(q, np.float64).reshape(-1, m["dof"])
-    C = sphere_centres(robot, q)
+    C = model_sphere_centres(m, q)
     R = np.array([s["r"] for s in m["spheres"]])
     leaves = sorted({l for g in m["env_groups"] for l in g["leaves"]})
     best = np.full(len(q), np.inf)

@@ -1,8 +1,8 @@
 """Differentiable clearance on the GPU (prrtc_path_cost_grad,
 prrtc_smooth_paths) against the oracle.
 
-Inputs are planned paths: Panda tabletop and shelf and Baxter tabletop queries
-solved by the batched planner, resampled to 64 float32 waypoints.  The
+Inputs are planned paths: Panda tabletop and shelf, Baxter tabletop and Fetch
+mixed-clutter queries solved by the batched planner, resampled to 64 float32 waypoints.  The
 library's adjoint must match the oracle's float64 adjoint to 1e-4 (relative,
 per waypoint, plus 1e-9 absolute for waypoints whose gradient vanishes) and the
 central finite differences of the library's own cost at h = 1e-3 rad within
@@ -35,6 +35,8 @@ def planned(ctx):
                   Settings(granularity=128, balance=2, tree_ratio=1.0, dynamic_domain=True, range=0.5)),
         "baxter": ([scenes.make_query("baxter", "tabletop", i, z_offset=0.3) for i in range(24)],
                    Settings(granularity=128, balance=1, tree_ratio=0.5)),
+        # Fetch: the robot with a prismatic joint (torso lift), mixed clutter
+        "fetch": ([scenes.make_query("fetch", "mixed", 300 + i, 30) for i in range(32)], Settings(granularity=64)),
     }
     for robot, (qs, s) in plan.items():
         res = ctx.solve_batch(robot, qs, BatchSettings(s, margin=1e-5), path_capacity=4096)
@@ -51,7 +53,7 @@ def planned(ctx):
     return out
 
 
-@pytest.mark.parametrize("robot", ["panda", "baxter"])
+@pytest.mark.parametrize("robot", ["panda", "baxter", "fetch"])
 def test_adjoint_matches_fp64(ctx, oracle, planned, robot):
     envs, P = planned[robot]
     cost, grad = ctx.path_cost_grad(robot, envs, P, MARGIN)

@@ -67,9 +67,14 @@ def rpy_of(R):
     return 0.0, p, math.atan2(-R[0, 1], R[1, 1])
 
 
-def test_panda_round_trip():
+def panda_round_trip(reference_pairs_only: bool = False):
     """Panda's fitted model written out as a URDF (joint origins from F, axis
-    z) and read back gives the same sphere kinematics."""
+    z) and read back: (the model built from the URDF, Panda's model, the
+    index of each URDF-model leaf in Panda's sphere list).  With
+    reference_pairs_only, link pairs that pRRTC's Panda model never checks
+    against each other are passed as allowed (as an SRDF's disabled
+    collisions would be), so only the link pairs pRRTC checks are checked,
+    and only pRRTC's leaf spheres become collision geometry."""
     from prrtc_gb300.robots import urdf
     from prrtc_gb300.robots.codegen import load_model
     pm = load_model("panda")
@@ -85,14 +90,32 @@ def test_panda_round_trip():
                      f'<axis xyz="0 0 1"/><limit lower="-3" upper="3"/></joint>')
     parts.append("</robot>")
     spheres = {}
-    for s in pm["spheres"]:
+    leaf_set = {i for g in pm["env_groups"] for i in g["leaves"]}
+    for i, s in enumerate(pm["spheres"]):
+        if reference_pairs_only and i not in leaf_set:
+            continue          # pRRTC's gate spheres bound leaves; they are not collision geometry
         spheres.setdefault(link[s["frame"]], []).append([*s["c"], s["r"]])
-    m = urdf.build_model("".join(parts), spheres, "panda_rt")
+    allowed = []
+    if reference_pairs_only:
+        sp = pm["spheres"]
+        checked = {frozenset((link[sp[a]["frame"]], link[sp[b]["frame"]]))
+                   for g in pm["self_groups"] for a, b in g["pairs"]}
+        names = list(link.values())
+        allowed = [(a, b) for i, a in enumerate(names) for b in names[i + 1:] if frozenset((a, b)) not in checked]
+    m = urdf.build_model("".join(parts), spheres, "panda_rt", allowed=allowed)
     src = {}
     for i, s in enumerate(pm["spheres"]):
-        src.setdefault(link[s["frame"]], []).append(i)
+        if not reference_pairs_only or i in leaf_set:
+            src.setdefault(link[s["frame"]], []).append(i)
     doc_order = ["world"] + [link[j["q"]] for j in pm["joints"]]   # the URDF's link order
-    idx = [k for l in doc_order for k in src.get(l, [])]
+    idx = [k for lk in doc_order for k in src.get(lk, [])]
+    return m, pm, idx
+
+
+def test_panda_round_trip():
+    """Panda's fitted model written out as a URDF and read back gives the
+    same sphere kinematics."""
+    m, pm, idx = panda_round_trip()
     leaves = [i for g in m["env_groups"] for i in g["leaves"]]
     assert len(leaves) == len(idx) == len(pm["spheres"])
     rng = np.random.default_rng(1)
