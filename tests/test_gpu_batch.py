@@ -138,3 +138,27 @@ def test_batch_idle_wait_limit_ends_run_with_error(ctx, oracle):
     b.free()
     res = ctx.solve_batch("panda", queries("panda", "tabletop", 8, 900), BatchSettings(c0()))
     assert all(r.solved for r in res)
+
+
+def test_batched_and_plain_success_agree(ctx, oracle):
+    """The batched form solves the queries the plain (drop-in) form solves:
+    on 48 Panda shelf queries with pRRTC's shelf settings (granularity 128,
+    balance 2, tree_ratio 1, dynamic domain), both success rates are reported
+    and the batched one may trail the plain one by at most two queries;
+    every path of both revalidates."""
+    from prrtc_gb300 import BatchSettings, Settings, scenes
+    s = Settings(granularity=128, balance=2, tree_ratio=1.0, dynamic_domain=True, dd_radius=4.0, dd_alpha=1e-4,
+                 dd_min_radius=1.0)
+    qs = [scenes.make_query("panda", "shelf", 2000 + i) for i in range(48)]
+    batched = ctx.solve_batch("panda", qs, BatchSettings(s, margin=1e-5, time_budget_ns=int(20e9)))
+    nb = check_all(oracle, "panda", qs, batched, 128, need_all=False)
+    ctx.set_planning_margin(1e-5)
+    ctx.set_time_budget(int(5e9))
+    plain = [ctx.solve("panda", q.start, q.goal, q.env, s) for q in qs]
+    ctx.set_time_budget(0)
+    ctx.set_planning_margin(0.0)
+    npl = check_all(oracle, "panda", qs, plain, 128, need_all=False)
+    costs = lambda rs: float(np.median([r.cost for r in rs if r.solved]))
+    print(f"48 shelf queries: batched solved {nb} (cost p50 {costs(batched):.2f}), plain solved {npl} "
+          f"(cost p50 {costs(plain):.2f})")
+    assert nb >= npl - 2
