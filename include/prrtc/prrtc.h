@@ -284,6 +284,9 @@ typedef struct prrtc_batch_settings {
                                         stats.error = 1 (0: 2^22, about a second) */
     int shared_frames;               /* 1: the checker keeps its forward-kinematics frames in each
                                         warp's shared memory; 0: in local memory (cached by L1) */
+    int rounds_per_header;           /* batches of 32 samples a warp may draw under one read of the
+                                        attempt's shared state while the early dynamic-domain test
+                                        rejects all of them (0: 1, at most 64) */
 } prrtc_batch_settings;
 
 typedef struct prrtc_batch prrtc_batch;

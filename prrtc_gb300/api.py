@@ -86,7 +86,8 @@ class BatchSettings(C.Structure):
                 ("blocks_per_sm", C.c_int),
                 ("use_graph", C.c_int),
                 ("margin", C.c_float), ("time_budget_ns", C.c_uint64), ("admission", C.c_int),
-                ("idle_wait_limit", C.c_uint32), ("shared_frames", C.c_int)]
+                ("idle_wait_limit", C.c_uint32), ("shared_frames", C.c_int),
+                ("rounds_per_header", C.c_int)]
 
     def __init__(self, plan: Settings | None = None, **kw):
         super().__init__()

@@ -758,57 +758,73 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
             continue;
         }
         {
-            // -- this lane's sample
-            const int k = k0 + lane;
-            const bool valid = (long long)k < P.max_samples_drawn;
-            const int vl = k % P.lanes;
-            const int iter = k / P.lanes + 1;
-            const int L = P.lanes;
-            int t;
-            if (P.balance == 0 || iter == 1) {
-                t = (vl < (L / 2)) ? 0 : 1;
-            } else if (P.balance == 1 && 2 * abs(f0 - f1) < 3 * L) {
-                const float ratio = f0 / (float)(f0 + f1);
-                t = ((float)vl < L * (1.0f - ratio)) ? 0 : 1;
-            } else if (P.balance == 1) {
-                const float ratio = f0 / (float)(f0 + f1);
-                t = ratio < P.tree_ratio ? 0 : 1;
-            } else {
-                // vamp balance (pRRTC.cu:364-371): a lane swaps trees unless the
-                // other is much larger.  The lane's previous tree is taken as
-                // alternating from its first choice, so no per-lane state is
-                // shared by the warps working on the attempt.
-                const int prev = ((iter - 1) + (vl < (L / 2) ? 0 : 1)) & 1;
-                const int ft = prev == 0 ? f0 : f1, fo = prev == 0 ? f1 : f0;
-                const float ratio = abs(ft - fo) / (float)ft;
-                t = ratio < P.tree_ratio ? 1 - prev : prev;
-            }
+            // -- this lane's sample.  While every lane's sample is rejected by
+            // the early test, the warp draws up to P.sub_rounds batches of 32
+            // under one round header: the next 32 tickets, the same tree sizes
+            // and, while the lanes keep choosing the same tree, the same
+            // staged domains (32 more of pRRTC's lanes reading one snapshot)
+            int k, vl, iter, t, t0, cnt0;
+            bool valid, early, rejected = false;
             float qv[D];
-            // dimensions in ceil(D / 7) equal groups, each group's digit chains interleaved
             constexpr int NG = (D + 6) / 7, G = (D + NG - 1) / NG;
-            const int t0 = __shfl_sync(FULL, t, 0);
-            const int cnt0 = min(t0 == 0 ? f0 : f1, P.cap);
-            const bool early = P.dynamic_domain && cnt0 <= 32 && __all_sync(FULL, t == t0);
             static_assert(G <= 7, "dimension groups of at most 7");
-            if (early)
-                stage_domains<G>(W, nodes_s + (size_t)t0 * D * P.cap, rad_s + (size_t)t0 * P.cap, P.cap, cnt0);
-            bool rejected = false;
-#pragma unroll
-            for (int d0 = 0; d0 < D; d0 += G) {
-                unsigned bs[G], as[G], hsh[G];
-                const int row = P.sampler == 0 ? (vl + attempt * P.lanes) % P.bases_lanes : vl % P.bases_lanes;
-#pragma unroll
-                for (int j = 0; j < G; j++) {
-                    const int d = d0 + j < D ? d0 + j : D - 1;   // a short last group repeats a dimension
-                    bs[j] = (unsigned)P.halton_bases[row * 16 + d];
-                    hsh[j] = P.sampler == 0 ? 0u : W.hsh[d];
-                    as[j] = 1u + hsh[j] - div_by(hsh[j], kDivTable.magic[bs[j] - 1u]) * (bs[j] - 1u);
+            int staged_t = -1;
+            for (int sub = 0;; sub++) {
+                k = k0 + lane;
+                valid = (long long)k < P.max_samples_drawn;
+                vl = k % P.lanes;
+                iter = k / P.lanes + 1;
+                const int L = P.lanes;
+                if (P.balance == 0 || iter == 1) {
+                    t = (vl < (L / 2)) ? 0 : 1;
+                } else if (P.balance == 1 && 2 * abs(f0 - f1) < 3 * L) {
+                    const float ratio = f0 / (float)(f0 + f1);
+                    t = ((float)vl < L * (1.0f - ratio)) ? 0 : 1;
+                } else if (P.balance == 1) {
+                    const float ratio = f0 / (float)(f0 + f1);
+                    t = ratio < P.tree_ratio ? 0 : 1;
+                } else {
+                    // vamp balance (pRRTC.cu:364-371): a lane swaps trees unless the
+                    // other is much larger.  The lane's previous tree is taken as
+                    // alternating from its first choice, so no per-lane state is
+                    // shared by the warps working on the attempt.
+                    const int prev = ((iter - 1) + (vl < (L / 2) ? 0 : 1)) & 1;
+                    const int ft = prev == 0 ? f0 : f1, fo = prev == 0 ? f1 : f0;
+                    const float ratio = abs(ft - fo) / (float)ft;
+                    t = ratio < P.tree_ratio ? 1 - prev : prev;
                 }
-                const bool e = early && d0 == 0;
-                const unsigned it = (unsigned)iter;
-                rejected = P.sampler == 0 ? sample_group<D, G, false>(P, W, it, d0, bs, as, hsh, e, cnt0, valid, qv)
-                                          : sample_group<D, G, true>(P, W, it, d0, bs, as, hsh, e, cnt0, valid, qv);
-                if (rejected) break;
+                // dimensions in ceil(D / 7) equal groups, each group's digit chains interleaved
+                t0 = __shfl_sync(FULL, t, 0);
+                cnt0 = min(t0 == 0 ? f0 : f1, P.cap);
+                early = P.dynamic_domain && cnt0 <= 32 && __all_sync(FULL, t == t0);
+                if (early && staged_t != t0) {
+                    stage_domains<G>(W, nodes_s + (size_t)t0 * D * P.cap, rad_s + (size_t)t0 * P.cap, P.cap, cnt0);
+                    staged_t = t0;
+                }
+                rejected = false;
+#pragma unroll
+                for (int d0 = 0; d0 < D; d0 += G) {
+                    unsigned bs[G], as[G], hsh[G];
+                    const int row = P.sampler == 0 ? (vl + attempt * P.lanes) % P.bases_lanes : vl % P.bases_lanes;
+#pragma unroll
+                    for (int j = 0; j < G; j++) {
+                        const int d = d0 + j < D ? d0 + j : D - 1;   // a short last group repeats a dimension
+                        bs[j] = (unsigned)P.halton_bases[row * 16 + d];
+                        hsh[j] = P.sampler == 0 ? 0u : W.hsh[d];
+                        as[j] = 1u + hsh[j] - div_by(hsh[j], kDivTable.magic[bs[j] - 1u]) * (bs[j] - 1u);
+                    }
+                    const bool e = early && d0 == 0;
+                    const unsigned it = (unsigned)iter;
+                    rejected = P.sampler == 0 ? sample_group<D, G, false>(P, W, it, d0, bs, as, hsh, e, cnt0, valid, qv)
+                                              : sample_group<D, G, true>(P, W, it, d0, bs, as, hsh, e, cnt0, valid, qv);
+                    if (rejected) break;
+                }
+                if (!rejected || sub + 1 >= P.sub_rounds) break;
+                int k1 = 0;
+                if (lane == 0) k1 = atomicAdd(&S->ticket, 32);
+                k1 = __shfl_sync(FULL, k1, 0);
+                if ((long long)k1 >= P.max_samples_drawn) break;   // the next header ends the attempt
+                k0 = k1;
             }
             if (!rejected) {
                 // -- nearest node of every lane's sample: one pass per tree, nodes

@@ -148,6 +148,7 @@ struct BatchParams {
     unsigned long long restart_after_ns;   // a query may get its k-th extra attempt after k x this
     unsigned idle_limit;                   // polls before an idle warp gives up (error flag)
     int shared_frames;                     // the checker's frames in the warp's shared memory (else local)
+    int sub_rounds;                        // 32-sample batches a round may draw while all are rejected early
     const float *cfg_pool;
     const BatchQueryDesc *queries;
     const int *order;    // admission order (query ids), null: index order
