@@ -245,8 +245,9 @@ __device__ __forceinline__ Frame relative_frame(const Frame &A, const Frame &B)
 // Where a table-form checker keeps its frames (F[0] the world, F[q + 1] the
 // frame of joint q) while it walks the schedule.
 //
-// LocalFrames: an array per thread.  The schedule indexes it with table
-// values, so it lives in local memory, cached by L1 while it fits there.
+// LocalFrames: an array per thread (frames 1 .. N-1; the world frame is a
+// constant).  The schedule indexes it with table values, so it lives in
+// local memory, cached by L1 while it fits there.
 //
 // SharedFrames: one column per lane in a warp's shared-memory area, float4
 // k (0..2) of frame i (i >= 1) at p[(3 (i - 1) + k) * 32], p = area + lane.
@@ -255,8 +256,11 @@ __device__ __forceinline__ Frame relative_frame(const Frame &A, const Frame &B)
 // world frame is not stored.  shared_frame_bytes(N) is a warp's area.
 template <int N>
 struct LocalFrames {
-    Frame F[N];
-    __device__ __forceinline__ void set(int i, const Frame &f) { F[i] = f; }
+    Frame F[N > 1 ? N - 1 : 1];   // the world frame is not stored
+    __device__ __forceinline__ void set(int i, const Frame &f)
+    {
+        if (i > 0) F[i - 1] = f;
+    }
     __device__ __forceinline__ const Frame *view() const { return F; }
 };
 
@@ -278,11 +282,17 @@ __host__ __device__ constexpr size_t shared_frame_bytes(int frames)
     return (size_t)(frames > 1 ? frames - 1 : 0) * 3 * 32 * sizeof(float4);
 }
 
-__device__ __forceinline__ Frame frame_at(const Frame *F, int i) { return F[i]; }
+__device__ __forceinline__ Frame world_frame()
+{
+    return Frame{{1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f}};
+}
+
+// frame i of a local array holding frames 1 .. N-1 (LocalFrames::view)
+__device__ __forceinline__ Frame frame_at(const Frame *F, int i) { return i == 0 ? world_frame() : F[i - 1]; }
 
 __device__ __forceinline__ Frame frame_at(const SharedFrames F, int i)
 {
-    if (i == 0) return Frame{{1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f}};
+    if (i == 0) return world_frame();
     const float4 *q = F.p + 3 * (i - 1) * 32;
     const float4 a = q[0], b = q[32], c = q[64];
     return Frame{{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w}};
