@@ -541,6 +541,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
     int slot = -1;
     int cq = 0, catt = 0;   // the slot's query and attempt, read when this warp takes the slot
     bool fresh = true;
+    bool trapped = false;   // this warp's last round on its slot was rejected early in full
     unsigned idle = 0;
     const float4 *staged = nullptr;   // the global records now in W_env
     unsigned long long nn_visits = 0;   // flushed once per warp (a shared counter would serialise)
@@ -698,6 +699,7 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                                      (unsigned)lane * 0x85EBCA77u + 0x165667B1u);
             __syncwarp();
             fresh = false;
+            trapped = false;
         }
         const int q = cq, attempt = catt;
         const BatchQueryDesc Qd = P.queries[q];
@@ -723,15 +725,20 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
         float *rad_s = P.radii + (size_t)slot * 2 * P.cap;
 
         // the round's shared state in one batch of independent loads: the slot's
-        // and the query's states, the tree sizes and 32 sample tickets (taken
-        // even when the attempt turns out to have ended: a ticket is only a count)
+        // and the query's states, the tree sizes and the round's sample
+        // tickets (taken even when the attempt turns out to have ended: a
+        // ticket is only a count).  A warp whose last round here was rejected
+        // early in full takes tickets for P.sub_rounds batches at once, so the
+        // warps sampling a trapped attempt share one atomic per sub_rounds x 32
+        // samples; tickets a round does not use are skipped samples.
+        const int take = trapped ? 32 * P.sub_rounds : 32;
         int k0 = 0, sst = 0, qst = 0, f0 = 0, f1 = 0;
         if (lane == 0) {
             sst = vload(&S->state);
             qst = vload(&P.qstate[q].state);
             f0 = vload(&S->free_index[0]);
             f1 = vload(&S->free_index[1]);
-            k0 = atomicAdd(&S->ticket, 32);
+            k0 = atomicAdd(&S->ticket, take);
         }
         sst = __shfl_sync(FULL, sst, 0);
         qst = __shfl_sync(FULL, qst, 0);
@@ -820,12 +827,15 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                     if (rejected) break;
                 }
                 if (!rejected || sub + 1 >= P.sub_rounds) break;
-                int k1 = 0;
-                if (lane == 0) k1 = atomicAdd(&S->ticket, 32);
-                k1 = __shfl_sync(FULL, k1, 0);
+                int k1 = k0 + 32;
+                if (take == 32) {   // the first trapped round: the next tickets one batch at a time
+                    if (lane == 0) k1 = atomicAdd(&S->ticket, 32);
+                    k1 = __shfl_sync(FULL, k1, 0);
+                }
                 if ((long long)k1 >= P.max_samples_drawn) break;   // the next header ends the attempt
                 k0 = k1;
             }
+            trapped = rejected && P.sub_rounds > 1;
             if (!rejected) {
                 // -- nearest node of every lane's sample: one pass per tree, nodes
                 // staged 32 at a time in shared memory and read by all lanes
