@@ -286,7 +286,7 @@ typedef struct prrtc_batch_settings {
                                         warp's shared memory; 0: in local memory (cached by L1) */
     int rounds_per_header;           /* batches of 32 samples a warp may draw under one read of the
                                         attempt's shared state while the early dynamic-domain test
-                                        rejects all of them (0: 1, at most 64) */
+                                        rejects all of them (0: 4, at most 64; 1: one batch per read) */
 } prrtc_batch_settings;
 
 typedef struct prrtc_batch prrtc_batch;

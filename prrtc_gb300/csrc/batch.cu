@@ -280,7 +280,7 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     P.restart_after_ns = settings->restart_after_ns ? settings->restart_after_ns : 10000000ull;
     P.idle_limit = settings->idle_wait_limit ? settings->idle_wait_limit : (1u << 22);
     P.shared_frames = settings->shared_frames ? 1 : 0;
-    P.sub_rounds = settings->rounds_per_header > 0 ? std::min(settings->rounds_per_header, 64) : 1;
+    P.sub_rounds = settings->rounds_per_header > 0 ? std::min(settings->rounds_per_header, 64) : 4;
     // pRRTC stops a query when any of its num_new_configs lanes passes max_iters
     // (pRRTC.cu:343-346), i.e. after about max_iters x num_new_configs samples
     // below 2^31 with room for the tickets that warps take after the last one
