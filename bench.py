@@ -353,6 +353,9 @@ def ours(args, rank, world):
     if args.clearance and robot == "panda":
         clearance = clearance_leg(ctx, O, qs, results, envs, baxter)
 
+    clocks = clk.summary()
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    theo = sm_count * 128 * 2 * clocks["sm_mhz"] * 1e6 / 1e12 if clocks.get("sm_mhz") else None
     single_med = statistics.median(single_ms)
     line = {
         "metric": metric_name(args), "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
@@ -384,6 +387,9 @@ def ours(args, rank, world):
                        "note": "Context.solve_batch: the Python wrapper's marshalling and unpacking included"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak,
+                     "peak_theoretical": theo, "frac_theoretical": achieved / theo if theo else None,
+                     "peak_theoretical_source": "SMs x 128 FP32 lanes x 2 FLOP x the median SM clock sampled "
+                                                "during the timed launch",
                      "traffic": (lambda b: b * len(qs) if b else None)(profiled_dram_bytes_per_query(args.workload)),
                      "traffic_source": "ncu capture of 256 queries (profiles/), scaled by queries processed",
                      "peak_source": "measured FP32 FMA chain kernel on this GPU (prrtc_measure_fp32_peak)",
@@ -398,7 +404,7 @@ def ours(args, rank, world):
                          "sample": f"the first {DIST_QUERIES} of the {len(qs)} queries, oracle RRT-Connect "
                                    f"restatement, {DIST_CPU_BUDGET_S:.0f} s per query"},
         "gpu_launches": launches,
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "other_workloads": others or None,
         "clearance": clearance,
     }
