@@ -394,6 +394,10 @@ def ours(args, rank, world):
                      "traffic_source": "ncu capture of 256 queries (profiles/), scaled by queries processed",
                      "peak_source": "measured FP32 FMA chain kernel on this GPU (prrtc_measure_fp32_peak)",
                      "nn_scan_bytes_per_s": nn_bytes / (st["kernel_ns"] * 1e-9),
+                     "nn_scan_tflops": 3 * plan_dof(robot) * st["nn_nodes"] / (st["kernel_ns"] * 1e-9) / 1e12,
+                     "nn_scan_note": "nearest-node passes: 4 D bytes and 3 D FLOPs per node visited and sample; "
+                                     "nodes are staged in shared memory 32 at a time and serve all 32 samples "
+                                     "of a round, from L2 (the trees stay L2-resident)",
                      "bulk": ({"achieved": st["bulk_flops"] / (st["bulk_ns"] * 1e-9) / 1e12,
                                "frac": st["bulk_flops"] / (st["bulk_ns"] * 1e-9) / 1e12 / peak,
                                "ms": st["bulk_ns"] / 1e6,

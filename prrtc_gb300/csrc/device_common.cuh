@@ -212,17 +212,15 @@ struct GenSched {
     int index;
 };
 struct GenEnvGroup {
-    float4 gate;          // gating sphere in its frame (x, y, z, r)
-    int gate_frame;       // -1 world; ignored when !has_gate
-    int has_gate;
-    int first_block, nblocks;
+    int gate;             // gating sphere: index into the gate centres, -1 none
+    int first_block, nblocks, pad_;
 };
 struct GenLeafBlock {
     int frame, first, n, pad_;
 };
 struct GenSelfGroup {
-    float4 a, b;          // gating pair, each in its frame
-    int fa, fb, first_block, nblocks;
+    int ga, gb;           // gating pair: indices into the gate centres
+    int first_block, nblocks;
 };
 struct GenPairBlock {
     int fa, fb, first, n;
@@ -354,8 +352,19 @@ struct FrameStore<Ctx, N, true> : SharedFrames {
 
 // The schedule of a table-form checker (see GenSched); returns true when free.
 // F is a frame view: a local array (const Frame *) or SharedFrames.
+// A gate sphere (x, y, z, r in frame T) in world coordinates, radius kept.
+__device__ __forceinline__ float4 gate_centre(const Frame &T, float4 c)
+{
+    float x, y, z;
+    xform(T, c, x, y, z);
+    return make_float4(x, y, z, c.w);
+}
+
+// G: the world centres of the gate spheres, computed with the frames (the
+// same xform as a leaf's, so verdicts do not change).
 template <class Frames, class Ctx>
-__device__ __noinline__ bool run_schedule(const Frames F, const GenSched *__restrict__ sched, int nsched,
+__device__ __noinline__ bool run_schedule(const Frames F, const float4 *__restrict__ G, const GenSched *__restrict__ sched,
+                                          int nsched,
                                           const GenEnvGroup *__restrict__ eg, const GenLeafBlock *__restrict__ lb,
                                           const float4 *__restrict__ leaves, const GenSelfGroup *__restrict__ sg,
                                           const GenPairBlock *__restrict__ pb, const LeafPair *__restrict__ pairs,
@@ -366,10 +375,9 @@ __device__ __noinline__ bool run_schedule(const Frames F, const GenSched *__rest
         if (e.kind == 0) {
             const GenEnvGroup g = eg[e.index];
             bool go = true;
-            if (g.has_gate) {
-                float x, y, z;
-                xform(frame_at(F, g.gate_frame + 1), g.gate, x, y, z);
-                go = ctx.env_hit(x, y, z, g.gate.w);
+            if (g.gate >= 0) {
+                const float4 c = G[g.gate];
+                go = ctx.env_hit(c.x, c.y, c.z, c.w);
             }
             if (go)
                 for (int k = g.first_block; k < g.first_block + g.nblocks; k++) {
@@ -378,10 +386,8 @@ __device__ __noinline__ bool run_schedule(const Frames F, const GenSched *__rest
                 }
         } else {
             const GenSelfGroup g = sg[e.index];
-            float ax, ay, az, bx, by, bz;
-            xform(frame_at(F, g.fa + 1), g.a, ax, ay, az);
-            xform(frame_at(F, g.fb + 1), g.b, bx, by, bz);
-            if (ctx.pair_hit(ax - bx, ay - by, az - bz, g.a.w + g.b.w))
+            const float4 a = G[g.ga], b = G[g.gb];
+            if (ctx.pair_hit(a.x - b.x, a.y - b.y, a.z - b.z, a.w + b.w))
                 for (int k = g.first_block; k < g.first_block + g.nblocks; k++) {
                     const GenPairBlock b = pb[k];
                     if (ctx.self_pairs(relative_frame(frame_at(F, b.fa + 1), frame_at(F, b.fb + 1)), pairs + b.first, b.n))

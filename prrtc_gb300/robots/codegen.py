@@ -321,6 +321,15 @@ def emit_cuda_checker(m: dict) -> str:
 
     table = name in TABLE_ROBOTS
     inline = not table or name in INLINE_VALIDATE
+    # the gate spheres (environment groups' bounding spheres and self groups'
+    # bounding pairs), each once, in order of first use
+    gate_ids = {}
+    for g in m["env_groups"]:
+        if g["gate"] >= 0:
+            gate_ids.setdefault(g["gate"], len(gate_ids))
+    for g in m["self_groups"]:
+        for sidx in g["gate"]:
+            gate_ids.setdefault(sidx, len(gate_ids))
     tcode = None
     if table:
         # every frame, in chain order, into F[q + 1]; then the schedule loop
@@ -330,7 +339,13 @@ def emit_cuda_checker(m: dict) -> str:
         code.lines.append("F.set(0, Frame{{1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 1.0f, 0.0f}});")
         for jt, T in zip(m["joints"], frames):
             code.lines.append(f"F.set({jt['q'] + 1}, {_frame_arg(T)});")
-        code.lines.append(f"return run_schedule(F.view(), k{R}Sched, {len(m['schedule'])}, k{R}EnvGroup, k{R}LeafBlock, k{R}Leaf, "
+        # gate centres in world coordinates, from the frames still in registers
+        # (the schedule walk then reads 16 bytes per gate test, not a frame)
+        fexpr = {-1: "world_frame()"} | {jt["q"]: _frame_arg(T) for jt, T in zip(m["joints"], frames)}
+        code.lines.append(f"float4 G[{max(1, len(gate_ids))}];")
+        for sidx, gid in gate_ids.items():
+            code.lines.append(f"G[{gid}] = gate_centre({fexpr[sp[sidx]['frame']]}, k{R}Gate[{gid}]);")
+        code.lines.append(f"return run_schedule(F.view(), G, k{R}Sched, {len(m['schedule'])}, k{R}EnvGroup, k{R}LeafBlock, k{R}Leaf, "
                           f"k{R}SelfGroup, k{R}PairBlock, k{R}Pair, ctx);")
         tcode = code
         code = _Code()              # the straight-line form, if any, goes to its own code
@@ -418,14 +433,16 @@ def emit_cuda_checker(m: dict) -> str:
             first = len(lblocks)
             for f, fl, n in env_blocks[gi]:
                 lblocks.append((f, fl, n))
-            if g["gate"] >= 0:
-                s = sp[g["gate"]]
-                eg_rows.append(((s["c"][0], s["c"][1], s["c"][2], s["r"]), s["frame"], 1, first, len(lblocks) - first))
-            else:
-                eg_rows.append(((0.0, 0.0, 0.0, 0.0), -1, 0, first, len(lblocks) - first))
+            eg_rows.append((gate_ids[g["gate"]] if g["gate"] >= 0 else -1, first, len(lblocks) - first))
+        w("// gate spheres (x, y, z, r) in their frames; gate_centre() puts them in the world")
+        w(f"__device__ const float4 k{R}Gate[{max(1, len(gate_ids))}] = {{")
+        for sidx in gate_ids or [None]:
+            c = sp[sidx] if sidx is not None else {"c": [0.0, 0.0, 0.0], "r": 0.0}
+            w("    {%s, %s, %s, %s}," % (*[_lit(v) for v in c["c"]], _lit(c["r"])))
+        w("};")
         w(f"__device__ const GenEnvGroup k{R}EnvGroup[{max(1, len(eg_rows))}] = {{")
-        for gate, f, has, first, nb in eg_rows or [((0.0, 0.0, 0.0, 0.0), -1, 0, 0, 0)]:
-            w("    {{%s}, %d, %d, %d, %d}," % (", ".join(_lit(v) for v in gate), f, has, first, nb))
+        for gid, first, nb in eg_rows or [(-1, 0, 0)]:
+            w(f"    {{{gid}, {first}, {nb}, 0}},")
         w("};")
         w(f"__device__ const GenLeafBlock k{R}LeafBlock[{max(1, len(lblocks))}] = {{")
         for f, fl, n in lblocks or [(-1, 0, 0)]:
@@ -437,12 +454,10 @@ def emit_cuda_checker(m: dict) -> str:
             for fa, fb, pf, n in self_blocks[gi]:
                 pblocks.append((fa, fb, pf, n))
             a, b = g["gate"]
-            sa, sb = sp[a], sp[b]
-            sg_rows.append(((*sa["c"], sa["r"]), (*sb["c"], sb["r"]), sa["frame"], sb["frame"], first, len(pblocks) - first))
+            sg_rows.append((gate_ids[a], gate_ids[b], first, len(pblocks) - first))
         w(f"__device__ const GenSelfGroup k{R}SelfGroup[{max(1, len(sg_rows))}] = {{")
-        for ga, gb, fa, fb, first, nb in sg_rows or [((0.0,) * 4, (0.0,) * 4, -1, -1, 0, 0)]:
-            w("    {{%s}, {%s}, %d, %d, %d, %d}," % (", ".join(_lit(v) for v in ga), ", ".join(_lit(v) for v in gb),
-                                                   fa, fb, first, nb))
+        for ga, gb, first, nb in sg_rows or [(0, 0, 0, 0)]:
+            w(f"    {{{ga}, {gb}, {first}, {nb}}},")
         w("};")
         w(f"__device__ const GenPairBlock k{R}PairBlock[{max(1, len(pblocks))}] = {{")
         for fa, fb, pf, n in pblocks or [(-1, -1, 0, 0)]:
