@@ -39,6 +39,12 @@ struct alignas(16) WarpScratch {
     float rad2[32];        // early rejection: the staged nodes' squared widened domain radii
     float box_lo[8], box_hi[8];   // and the box around all their domains
     unsigned hsh[16];      // scrambled sampler: the hash of (query, attempt, dimension)
+    // the round's samples that survive the dynamic-domain test, per lane:
+    // coordinates, tree, nearest node, Halton iteration and distance (kept
+    // here rather than in registers across the edge checks)
+    float pend_q[D][32];
+    int pend_t[32], pend_i[32], pend_it[32];
+    float pend_d[32];
     int bad;
 };
 
@@ -874,20 +880,25 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
                 bool go = valid;
                 if (go && P.dynamic_domain) go = !(__ldcg(rad_s + (size_t)t * P.cap + bi) < dist);
                 unsigned todo = __ballot_sync(FULL, go);
+                if (go) {
+#pragma unroll
+                    for (int d = 0; d < D; d++) W.pend_q[d][lane] = qv[d];
+                    W.pend_t[lane] = t;
+                    W.pend_i[lane] = bi;
+                    W.pend_it[lane] = iter;
+                    W.pend_d[lane] = dist;
+                }
+                __syncwarp();
 
                 // -- extend (and connect) each surviving sample, in lane order
                 while (todo) {
                     const int j = __ffs(todo) - 1;
                     todo &= todo - 1;
-                    const int tj = __shfl_sync(FULL, t, j);
-                    const int ni = __shfl_sync(FULL, bi, j);
-                    const int iterj = __shfl_sync(FULL, iter, j);
-                    const float distj = __shfl_sync(FULL, dist, j);
-#pragma unroll
-                    for (int d = 0; d < D; d++) {
-                        const float v = __shfl_sync(FULL, qv[d], j);
-                        if (lane == d) W.cfg[d] = v;
-                    }
+                    const int tj = W.pend_t[j];
+                    const int ni = W.pend_i[j];
+                    const int iterj = W.pend_it[j];
+                    const float distj = W.pend_d[j];
+                    if (lane < D) W.cfg[lane] = W.pend_q[lane][j];
                     const int o = 1 - tj;
                     float *nd_t = nodes_s + (size_t)tj * D * P.cap, *nd_o = nodes_s + (size_t)o * D * P.cap;
                     int *pr_t = par_s + (size_t)tj * P.cap;
