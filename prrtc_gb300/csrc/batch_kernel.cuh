@@ -33,9 +33,18 @@ namespace prrtc {
 // memory through L1.
 template <int D>
 struct alignas(16) WarpScratch {
+    static constexpr int kPairQuads = (D + 1) / 2;              // float4 holding a staged node pair
+    static constexpr int kPairStride = kPairQuads | 1;         // odd: staging stores conflict at most 2-way
+    static constexpr int kTreeQuads = 16 * kPairStride + 1;    // per tree (+1: the trees' pairs in other banks)
+    union {
+        // early rejection: the first coordinates of the staged nodes (+1: bank skew)
+        float chunk[D][33];
+        // the nearest-node pass: 32 nodes of each tree as 16 node pairs, pair p
+        // of tree t at nnp[t * kTreeQuads + p * kPairStride + k], k < kPairQuads,
+        // holding (x_2k of node 2p, of node 2p + 1, x_2k+1 of node 2p, of node 2p + 1)
+        float4 nnp[2 * kTreeQuads];
+    };
     float from[D], step[D], cfg[D], nn[D], vec[D], next[D];
-    float chunk[D][33];    // 32 tree nodes staged for the round's nearest-neighbour pass (+1: bank skew);
-                           // early rejection stages its nodes' first coordinates here before that pass
     float rad2[32];        // early rejection: the staged nodes' squared widened domain radii
     float box_lo[8], box_hi[8];   // and the box around all their domains
     unsigned hsh[16];      // scrambled sampler: the hash of (query, attempt, dimension)
@@ -843,38 +852,63 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
             }
             trapped = rejected && P.sub_rounds > 1;
             if (!rejected) {
-                // -- nearest node of every lane's sample: one pass per tree, nodes
-                // staged 32 at a time in shared memory and read by all lanes
+                // -- nearest node of every lane's sample: both trees in one pass,
+                // 32 nodes of each staged per step in shared memory as node pairs;
+                // a lane scans its own tree's chunk, two nodes per packed FP32
+                // instruction (__fadd2_rn / __ffma2_rn: each half computes the
+                // same operations as the scalar form, fsub then fmaf over the
+                // dimensions in order), nodes in index order, so the nearest
+                // node and its distance are the scalar scan's
                 float best = FLT_MAX;
                 int bi = 0;
-                for (int tree = 0; tree < 2; tree++) {
-                    if (!__any_sync(FULL, valid && t == tree)) continue;
-                    const int cnt = min(tree == 0 ? f0 : f1, P.cap);
-                    const float *nd = nodes_s + (size_t)tree * D * P.cap;
-                    for (int base = 0; base < cnt; base += 32) {
+                {
+                    constexpr int PQ = WarpScratch<D>::kPairQuads, PS = WarpScratch<D>::kPairStride,
+                                  TQ = WarpScratch<D>::kTreeQuads;
+                    const bool act0 = __any_sync(FULL, valid && t == 0), act1 = __any_sync(FULL, valid && t == 1);
+                    const int cnt0 = act0 ? min(f0, P.cap) : 0, cnt1 = act1 ? min(f1, P.cap) : 0;
+                    const int cmax = max(cnt0, cnt1);
+                    float2 nq[2 * PQ];   // -q twice per dimension (x - q == x + (-q) exactly)
+#pragma unroll
+                    for (int d = 0; d < 2 * PQ; d++) nq[d] = d < D ? make_float2(-qv[d], -qv[d]) : make_float2(0.0f, 0.0f);
+                    const float4 *mine = W.nnp + (t == 0 ? 0 : TQ);
+                    float *stage = reinterpret_cast<float *>(W.nnp + (lane >> 1) * PS) + (lane & 1);
+                    const float qnan = __int_as_float(0x7FFFFFFF);
+                    for (int base = 0; base < cmax; base += 32) {
                         const int i = base + lane;
 #pragma unroll
-                        for (int d = 0; d < D; d++)
-                            W.chunk[d][lane] = i < cnt ? __ldcg(nd + (size_t)d * P.cap + i) : __int_as_float(0x7FFFFFFF);
+                        for (int d = 0; d < D; d++) {
+                            const int o = (d >> 1) * 4 + (d & 1) * 2;
+                            stage[o] = i < cnt0 ? __ldcg(nodes_s + (size_t)d * P.cap + i) : qnan;
+                            stage[4 * TQ + o] = i < cnt1 ? __ldcg(nodes_s + (size_t)(D + d) * P.cap + i) : qnan;
+                        }
                         __syncwarp();
-                        if (valid && t == tree) {
-                            const int m = min(32, cnt - base);
-                            for (int n = 0; n < m; n++) {
-                                float a = 0.0f;
+                        const int pairs = (min(32, cmax - base) + 1) >> 1;
+                        for (int pr = 0; pr < pairs; pr++) {
+                            const float4 *r = mine + pr * PS;
+                            float2 a = make_float2(0.0f, 0.0f);
 #pragma unroll
-                                for (int d = 0; d < D; d++) {
-                                    const float x = W.chunk[d][n] - qv[d];
-                                    a = fmaf(x, x, a);
+                            for (int k = 0; k < PQ; k++) {
+                                const float4 v = r[k];
+                                const float2 x0 = __fadd2_rn(make_float2(v.x, v.y), nq[2 * k]);
+                                a = __ffma2_rn(x0, x0, a);
+                                if (2 * k + 1 < D) {
+                                    const float2 x1 = __fadd2_rn(make_float2(v.z, v.w), nq[2 * k + 1]);
+                                    a = __ffma2_rn(x1, x1, a);
                                 }
-                                if (a < best) {
-                                    best = a;
-                                    bi = base + n;
-                                }
+                            }
+                            if (a.x < best) {
+                                best = a.x;
+                                bi = base + 2 * pr;
+                            }
+                            if (a.y < best) {
+                                best = a.y;
+                                bi = base + 2 * pr + 1;
                             }
                         }
                         __syncwarp();
                     }
-                    nn_visits += (unsigned long long)cnt * __popc(__ballot_sync(FULL, valid && t == tree));
+                    nn_visits += (unsigned long long)cnt0 * __popc(__ballot_sync(FULL, valid && t == 0)) +
+                                 (unsigned long long)cnt1 * __popc(__ballot_sync(FULL, valid && t == 1));
                 }
                 const float dist = sqrtf(best);
                 bool go = valid;
