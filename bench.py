@@ -396,8 +396,8 @@ def ours(args, rank, world):
                      "nn_scan_bytes_per_s": nn_bytes / (st["kernel_ns"] * 1e-9),
                      "nn_scan_tflops": 3 * plan_dof(robot) * st["nn_nodes"] / (st["kernel_ns"] * 1e-9) / 1e12,
                      "nn_scan_note": "nearest-node passes: 4 D bytes and 3 D FLOPs per node visited and sample; "
-                                     "nodes are staged in shared memory 32 at a time and serve all 32 samples "
-                                     "of a round, from L2 (the trees stay L2-resident)",
+                                     "32 nodes of each tree are staged per step in shared memory and serve all "
+                                     "32 samples of a round, from L2 (the trees stay L2-resident)",
                      "bulk": ({"achieved": st["bulk_flops"] / (st["bulk_ns"] * 1e-9) / 1e12,
                                "frac": st["bulk_flops"] / (st["bulk_ns"] * 1e-9) / 1e12 / peak,
                                "ms": st["bulk_ns"] / 1e6,
