@@ -791,11 +791,18 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
             constexpr int NG = (D + 6) / 7, G = (D + NG - 1) / NG;
             static_assert(G <= 7, "dimension groups of at most 7");
             int staged_t = -1;
+            // a lane count that is a power of two divides by a shift
+            const int lshift = (P.lanes & (P.lanes - 1)) == 0 ? __ffs(P.lanes) - 1 : -1;
             for (int sub = 0;; sub++) {
                 k = k0 + lane;
                 valid = (long long)k < P.max_samples_drawn;
-                vl = k % P.lanes;
-                iter = k / P.lanes + 1;
+                if (lshift >= 0) {
+                    vl = k & (P.lanes - 1);
+                    iter = (k >> lshift) + 1;
+                } else {
+                    vl = k % P.lanes;
+                    iter = k / P.lanes + 1;
+                }
                 const int L = P.lanes;
                 if (P.balance == 0 || iter == 1) {
                     t = (vl < (L / 2)) ? 0 : 1;
