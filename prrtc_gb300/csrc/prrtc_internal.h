@@ -70,15 +70,19 @@ enum SlotStateCode { SLOT_FREE = 0, SLOT_RUNNING = 1, SLOT_DONE = 2, SLOT_BUSY =
 
 // One resident slot: an attempt at a query (its trees live in the arena at
 // the slot's index).
-struct SlotState {
+// Each slot owns two 128-byte lines: the sample ticket, taken by an atomic
+// in every round header of every warp working the slot, on the second, so
+// that those atomics neither queue the reads of the slot's state nor touch
+// the lines of other slots.
+struct alignas(128) SlotState {
     int query;
     int attempt;         // attempt number of the query (selects its sample stream)
     int state;           // SlotStateCode
     int free_index[2];
-    int ticket;          // samples drawn so far
     int workers;         // warps registered on the slot
     int restart;         // 1: the warp that recycles the slot restarts the query here
     unsigned long long t_start;   // device ns when the slot's attempt was admitted
+    alignas(128) int ticket;      // samples drawn so far
 };
 
 // Per-query state shared by its attempts.
