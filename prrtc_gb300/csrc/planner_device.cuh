@@ -118,30 +118,41 @@ __device__ __forceinline__ void block_nn(const float *__restrict__ nodes, int ca
 }
 
 // Dynamic-domain updates with the reference's CAS loops (pRRTC.cu:456-468,
-// 584-598).  A failed CAS means another update landed, so every update ends
-// after at most as many retries as there are concurrent updaters; the loop is
-// still bounded (kDdTries, far above any block or warp count the planners
-// launch) so that no wait can be endless.
+// 584-598): each update is computed from the radius it replaces.  A failed
+// CAS returns the radius another update just wrote, which the next try
+// starts from (no second read).  A shrink of a radius already at the floor
+// (rmin) changes nothing and issues no CAS (trapped trees sit there).  A
+// failed CAS means another update landed, so every update ends after at most
+// as many retries as there are concurrent updaters; the loop is still
+// bounded (kDdTries, far above any block or warp count the planners launch)
+// so that no wait can be endless.
 constexpr int kDdTries = 1 << 16;
 
 __device__ __forceinline__ void dd_grow(float *r, float alpha)
 {
-    volatile float *rp = r;
+    int *ri = reinterpret_cast<int *>(r);
+    int cur = *(volatile int *)ri;
     for (int tries = 0; tries < kDdTries; tries++) {
-        const float old = *rp;
+        const float old = __int_as_float(cur);
         if (old == FLT_MAX) return;
         const float nw = old * (1.0f + alpha);
-        if (atomicCAS(reinterpret_cast<int *>(r), __float_as_int(old), __float_as_int(nw)) == __float_as_int(old)) return;
+        const int seen = atomicCAS(ri, cur, __float_as_int(nw));
+        if (seen == cur) return;
+        cur = seen;
     }
 }
 
 __device__ __forceinline__ void dd_shrink(float *r, float alpha, float radius0, float rmin)
 {
-    volatile float *rp = r;
+    int *ri = reinterpret_cast<int *>(r);
+    int cur = *(volatile int *)ri;
     for (int tries = 0; tries < kDdTries; tries++) {
-        const float old = *rp;
+        const float old = __int_as_float(cur);
         const float nw = (old == FLT_MAX) ? radius0 : fmaxf(old * (1.0f - alpha), rmin);
-        if (atomicCAS(reinterpret_cast<int *>(r), __float_as_int(old), __float_as_int(nw)) == __float_as_int(old)) return;
+        if (__float_as_int(nw) == cur) return;   // at the floor already: the update writes nothing new
+        const int seen = atomicCAS(ri, cur, __float_as_int(nw));
+        if (seen == cur) return;
+        cur = seen;
     }
 }
 
