@@ -21,10 +21,10 @@ __global__ void __launch_bounds__(64) k_path_cost_grad(ClrModel M, const ClrEnv 
                                                       float *__restrict__ cost, float *__restrict__ grad)
 {
     extern __shared__ float4 s_env[];
+    __shared__ unsigned long long s_bar;
     const int path = blockIdx.y;
     const ClrEnv pe = envs[path];
-    stage_env(s_env, pe.rec, pe.n.records());
-    __syncthreads();
+    stage_env_bulk(s_env, pe.rec, pe.n.records(), &s_bar);
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= waypoints) return;
     const size_t row = (size_t)path * waypoints + w;

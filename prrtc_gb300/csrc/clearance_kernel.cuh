@@ -39,16 +39,16 @@ __global__ void __launch_bounds__(128) k_smooth_paths(const ClrLaunch P)
     extern __shared__ float4 s_dyn[];
     __shared__ int s_bad;
     __shared__ float s_red[4];
+    __shared__ unsigned long long s_bar;
     const int path = blockIdx.x;
     const int W = P.waypoints;
     const ClrEnv pe = P.envs[path];
     const int R = pe.n.records();
     float *s_q = reinterpret_cast<float *>(s_dyn + R);
     float *s_g = s_q + W * D;
-    stage_env(s_dyn, pe.rec, R);
     float *gq = P.q + (size_t)path * W * D;
     for (int i = threadIdx.x; i < W * D; i += blockDim.x) s_q[i] = gq[i];
-    __syncthreads();
+    stage_env_bulk(s_dyn, pe.rec, R, &s_bar);   // synchronises the block
     const ClrEnv e{s_dyn, pe.n};
     const ClrSmooth s = P.s;
     CheckCtx ctx{EnvView{e.rec, e.n}, 0.0f, &s_bad};

@@ -43,6 +43,57 @@ __device__ __forceinline__ void stage_env(float4 *smem, const float4 *__restrict
     for (int i = threadIdx.x; i < records; i += blockDim.x) smem[i] = __ldg(g + i);
 }
 
+// The same copy as one bulk asynchronous copy by the SM's TMA engine
+// (cp.async.bulk global -> shared, no tensor map), completed on the
+// shared-memory mbarrier `bar`: thread 0 arms the barrier with the byte count
+// and issues the copy, every thread waits for the barrier's phase 0.  Both
+// addresses are 16-byte aligned (float4 records) and the size is a multiple
+// of 16 bytes, as the bulk copy requires.  All threads of the block call it,
+// once per kernel (the barrier's first phase); it returns with the records in
+// shared memory and the block synchronised.  The wait is bounded: should the
+// copy not complete within kBulkPolls polls, the block copies the records
+// itself (the same bytes) and, before it returns, polls once more so that no
+// copy can still be landing while the block goes on.
+constexpr int kBulkPolls = 1 << 20;
+
+__device__ __forceinline__ bool bulk_phase0_done(unsigned bar)
+{
+    unsigned done;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done)
+                 : "r"(bar)
+                 : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ void stage_env_bulk(float4 *smem, const float4 *__restrict__ g, int records,
+                                               unsigned long long *mbar)
+{
+    if (records <= 0) {
+        __syncthreads();
+        return;
+    }
+    const unsigned bytes = (unsigned)records * 16u;
+    const unsigned bar = (unsigned)__cvta_generic_to_shared(mbar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(g), "r"(bytes), "r"(bar)
+                     : "memory");
+    }
+    __syncthreads();   // the barrier is armed before anyone polls it
+    bool done = false;
+    for (int i = 0; i < kBulkPolls && !done; i++) done = bulk_phase0_done(bar);
+    if (!__syncthreads_and(done)) {
+        stage_env(smem, g, records);
+        for (int i = 0; i < kBulkPolls && !done; i++) done = bulk_phase0_done(bar);
+        __syncthreads();
+    }
+}
+
 // ---- the reference's primitive tests (src/planning/utils.cuh:58-209) ------
 // Each returns true when the sphere (x, y, z, r) intersects the primitive,
 // i.e. the reference's "< 0" on squared distance minus squared radius.

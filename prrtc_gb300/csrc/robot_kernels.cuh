@@ -41,8 +41,8 @@ __global__ void __launch_bounds__(256) k_validate_configs(const float4 *__restri
                                                           uint8_t *__restrict__ out, unsigned long long *work)
 {
     extern __shared__ float4 s_env[];
-    stage_env(s_env, env, nc.records());
-    __syncthreads();
+    __shared__ unsigned long long s_bar;
+    stage_env_bulk(s_env, env, nc.records(), &s_bar);
     CheckCtx ctx{{s_env, nc}, 0.0f, nullptr};
     unsigned long long flops = 0, cfgs = 0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -68,7 +68,8 @@ __global__ void __launch_bounds__(128) k_validate_edges(const float4 *__restrict
     extern __shared__ float4 s_env[];
     __shared__ float s_a[D], s_step[D];
     __shared__ int s_bad;
-    stage_env(s_env, env, nc.records());
+    __shared__ unsigned long long s_bar;
+    stage_env_bulk(s_env, env, nc.records(), &s_bar);
     CheckCtx ctx{{s_env, nc}, 0.0f, &s_bad};
     const float fg = (float)g;
     for (int64_t e = blockIdx.x; e < n; e += gridDim.x) {
@@ -103,8 +104,8 @@ __global__ void __launch_bounds__(128) k_goal_flags(const float4 *__restrict__ e
                                                     uint8_t *__restrict__ flags)
 {
     extern __shared__ float4 s_env[];
-    stage_env(s_env, env, nc.records());
-    __syncthreads();
+    __shared__ unsigned long long s_bar;
+    stage_env_bulk(s_env, env, nc.records(), &s_bar);
     CheckCtx ctx{{s_env, nc}, 0.0f, nullptr};
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < g.tries; t += (long long)gridDim.x * blockDim.x) {
         float q[Gen::kDof];
@@ -168,13 +169,13 @@ __global__ void __launch_bounds__(256) k_rrtc_plain(const PlainParams P)
     const int tid = threadIdx.x, bid = blockIdx.x;
     volatile QueryCtl *ctl = P.ctl;
 
-    stage_env(s_env, P.env, P.env_n.records());
+    __shared__ unsigned long long s_bar;
     if (tid < D) {
         s_hb[tid] = P.halton_bases[bid * 16 + tid];
         s_hn[tid] = 0.0f;
         s_hd[tid] = 1.0f;
     }
-    __syncthreads();
+    stage_env_bulk(s_env, P.env, P.env_n.records(), &s_bar);   // synchronises the block
     CheckCtx ctx{{s_env, P.env_n}, P.pad, &s_bad};
     const float fg = (float)P.granularity;
     const unsigned long long t0 = P.budget_ns ? global_ns() : 0ull;
