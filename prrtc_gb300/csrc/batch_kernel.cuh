@@ -54,6 +54,7 @@ struct alignas(16) WarpScratch {
     float pend_q[D][32];
     int pend_t[32], pend_i[32], pend_it[32];
     float pend_d[32];
+    unsigned long long env_bar;   // mbarrier of the bulk copies that stage the obstacle records
     int bad;
 };
 
@@ -559,6 +560,13 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
     bool trapped = false;   // this warp's last round on its slot was rejected early in full
     unsigned idle = 0;
     const float4 *staged = nullptr;   // the global records now in W_env
+    const unsigned env_bar = (unsigned)__cvta_generic_to_shared(&W.env_bar);
+    unsigned env_phase = 0;           // parity of W.env_bar's next phase
+    if (lane == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(env_bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
     unsigned long long nn_visits = 0;   // flushed once per warp (a shared counter would serialise)
     auto flush = [&]() {
         if (lane == 0 && nn_visits) atomicAdd(&C->nn_nodes, nn_visits);
@@ -721,8 +729,30 @@ __global__ void __launch_bounds__(128) k_rrtc_batch(const BatchParams P)
         const float4 *envp = Qd.env;
         if (Qd.env_n.records() <= P.env_records) {
             if (staged != Qd.env) {   // the records are read-only for the whole launch
+                // one bulk copy by the TMA engine into the warp's area, completed
+                // on the warp's mbarrier (after a proxy fence: the area was last
+                // read by the checker's ordinary loads); the wait is bounded, a
+                // plain copy of the same bytes behind it
                 __syncwarp();
-                for (int i = lane; i < Qd.env_n.records(); i += 32) W_env[i] = __ldg(Qd.env + i);
+                const unsigned bytes = (unsigned)Qd.env_n.records() * 16u;
+                if (bytes) {
+                    if (lane == 0) {
+                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(env_bar),
+                                     "r"(bytes)
+                                     : "memory");
+                        asm volatile(
+                            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                                (unsigned)__cvta_generic_to_shared(W_env)),
+                            "l"(Qd.env), "r"(bytes), "r"(env_bar)
+                            : "memory");
+                    }
+                    bool done = false;
+                    for (int i = 0; i < kBulkPolls && !done; i++) done = bulk_phase_done(env_bar, env_phase);
+                    env_phase ^= 1u;
+                    if (!__all_sync(FULL, done))
+                        for (int i = lane; i < Qd.env_n.records(); i += 32) W_env[i] = __ldg(Qd.env + i);
+                }
                 __syncwarp();
                 staged = Qd.env;
             }

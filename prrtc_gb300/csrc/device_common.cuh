@@ -56,13 +56,14 @@ __device__ __forceinline__ void stage_env(float4 *smem, const float4 *__restrict
 // copy can still be landing while the block goes on.
 constexpr int kBulkPolls = 1 << 20;
 
-__device__ __forceinline__ bool bulk_phase0_done(unsigned bar)
+// has the mbarrier at shared address `bar` completed its phase of parity `parity`?
+__device__ __forceinline__ bool bulk_phase_done(unsigned bar, unsigned parity)
 {
     unsigned done;
-    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
                  "selp.u32 %0, 1, 0, p;\n\t}"
                  : "=r"(done)
-                 : "r"(bar)
+                 : "r"(bar), "r"(parity)
                  : "memory");
     return done != 0;
 }
@@ -86,10 +87,10 @@ __device__ __forceinline__ void stage_env_bulk(float4 *smem, const float4 *__res
     }
     __syncthreads();   // the barrier is armed before anyone polls it
     bool done = false;
-    for (int i = 0; i < kBulkPolls && !done; i++) done = bulk_phase0_done(bar);
+    for (int i = 0; i < kBulkPolls && !done; i++) done = bulk_phase_done(bar, 0u);
     if (!__syncthreads_and(done)) {
         stage_env(smem, g, records);
-        for (int i = 0; i < kBulkPolls && !done; i++) done = bulk_phase0_done(bar);
+        for (int i = 0; i < kBulkPolls && !done; i++) done = bulk_phase_done(bar, 0u);
         __syncthreads();
     }
 }
