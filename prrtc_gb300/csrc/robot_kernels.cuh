@@ -35,8 +35,21 @@ __device__ __forceinline__ void add_work(unsigned long long *work, unsigned long
     }
 }
 
+// Launch bounds of the stand-alone configuration checker, per robot: by
+// default at most 64 registers (128-thread blocks, 8 per SM), where the
+// straight-line checker spills a little but 64 resident warps per SM instead
+// of 16 hide its dependency waits better (2^20 random configurations: Panda
+// 1.23 vs 1.27 ms on the tabletop scene and 1.81 vs 1.97 ms on the shelf,
+// Baxter 11.9 vs 14.0 ms); a robot file may specialise it (Fetch, 4.5 vs
+// 4.8 ms, keeps its 104 registers).
 template <class Gen>
-__global__ void __launch_bounds__(256) k_validate_configs(const float4 *__restrict__ env, EnvCounts nc,
+struct ValidateLaunch {
+    static constexpr int kMaxThreads = 128, kMinBlocks = 8;
+};
+
+template <class Gen>
+__global__ void __launch_bounds__(ValidateLaunch<Gen>::kMaxThreads, ValidateLaunch<Gen>::kMinBlocks)
+    k_validate_configs(const float4 *__restrict__ env, EnvCounts nc,
                                                           const float *__restrict__ q, int64_t n,
                                                           uint8_t *__restrict__ out, unsigned long long *work)
 {
