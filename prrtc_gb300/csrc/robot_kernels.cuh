@@ -37,7 +37,7 @@ __device__ __forceinline__ void add_work(unsigned long long *work, unsigned long
 
 // Launch bounds of the stand-alone configuration checker, per robot: by
 // default at most 64 registers (128-thread blocks, 8 per SM), where the
-// straight-line checker spills a little but 64 resident warps per SM instead
+// straight-line checker spills a little but 32 resident warps per SM instead
 // of 16 hide its dependency waits better (2^20 random configurations: Panda
 // 1.23 vs 1.27 ms on the tabletop scene and 1.81 vs 1.97 ms on the shelf,
 // Baxter 11.9 vs 14.0 ms); a robot file may specialise it (Fetch, 4.5 vs
