@@ -70,8 +70,12 @@ __global__ void __launch_bounds__(ValidateLaunch<Gen>::kMaxThreads, ValidateLaun
 }
 
 // One block per edge (grid-stride): thread t checks points k = t+1, t+1+blockDim, ...
-template <class Gen>
-__global__ void __launch_bounds__(128) k_validate_edges(const float4 *__restrict__ env, EnvCounts nc,
+// MinBlocks > 0 builds it for that many resident 128-thread blocks per SM: 8
+// (at most 64 registers) is faster for 128-point edges (the Panda shelf
+// scene at g = 128: 1.79 vs 1.91 ms for 2^14 edges) and slower for the
+// 32-thread blocks of short edges, which keep the unconstrained build (0).
+template <class Gen, int MinBlocks>
+__global__ void __launch_bounds__(128, MinBlocks) k_validate_edges(const float4 *__restrict__ env, EnvCounts nc,
                                                         const float *__restrict__ a, const float *__restrict__ b,
                                                         int64_t n, int g, uint8_t *__restrict__ out,
                                                         unsigned long long *work)
@@ -399,7 +403,10 @@ struct RobotKernels {
         int64_t blocks = n;
         const int64_t cap = (int64_t)le.sms * (2048 / threads);
         if (blocks > cap) blocks = cap;
-        k_validate_edges<Gen><<<(int)blocks, threads, smem, st>>>(le.rec, le.counts, a, b, n, g, out, le.work);
+        if (threads == 128)
+            k_validate_edges<Gen, 8><<<(int)blocks, threads, smem, st>>>(le.rec, le.counts, a, b, n, g, out, le.work);
+        else
+            k_validate_edges<Gen, 0><<<(int)blocks, threads, smem, st>>>(le.rec, le.counts, a, b, n, g, out, le.work);
         return cudaGetLastError();
     }
     static cudaError_t fk_spheres(const float *q, int64_t n, float *out, int sms, cudaStream_t st)
