@@ -306,10 +306,14 @@ class RefGpuChecker(_Cubin):
     def available(cls, robot: str) -> bool:
         return cls.path(robot).exists()
 
-    def check(self, env, q) -> np.ndarray:
-        """Reference verdicts (1 = free) for configurations q [n, dof]."""
+    def prepare(self, env, q):
+        """Builds the reference's Environment<float> for env on the device and
+        returns (run, out): run() launches the checker once on the current
+        stream over q (a host array or a CUDA tensor [n, dof]), writing
+        verdicts (1 = free) into the CUDA tensor out [n]."""
         torch = self.torch
-        q = torch.from_numpy(_arr(q, self.dim)).cuda()
+        q = q.contiguous() if hasattr(q, "data_ptr") else torch.from_numpy(_arr(q, self.dim)).cuda()
+        assert q.dtype == torch.float32 and q.is_cuda and q.shape[-1] == self.dim
         arrs = [torch.from_numpy(_arr(a, k)).cuda() for a, k in
                 ((env.spheres, 4), (env.capsules, 8), (env.z_aligned_capsules, 8), (env.cuboids, 15),
                  (env.z_aligned_cuboids, 15))]
@@ -327,12 +331,22 @@ class RefGpuChecker(_Cubin):
         self.launch("ref_env_build", 1, 1, eargs)
         n = len(q)
         out = torch.full((max(n, 1),), 255, dtype=torch.uint8, device="cuda")
-        if n:
-            self.launch(self.kname, (n + 127) // 128, 128,
-                        [C.c_void_p(q.data_ptr()), C.c_longlong(n), C.c_int(self.dim),
-                         C.c_void_p(scratch.data_ptr()), C.c_void_p(out.data_ptr())])
-        torch.cuda.synchronize()
-        res = out[:n].cpu().numpy()
+
+        def run():
+            # q, arrs and scratch stay alive through this closure
+            if n:
+                self.launch(self.kname, (n + 127) // 128, 128,
+                            [C.c_void_p(q.data_ptr()), C.c_longlong(n), C.c_int(self.dim),
+                             C.c_void_p(scratch.data_ptr()), C.c_void_p(out.data_ptr())])
+            return arrs
+        return run, out[:n]
+
+    def check(self, env, q) -> np.ndarray:
+        """Reference verdicts (1 = free) for configurations q [n, dof]."""
+        run, out = self.prepare(env, q)
+        run()
+        self.torch.cuda.synchronize()
+        res = out.cpu().numpy()
         assert np.all(res <= 1), "reference GPU checker left verdicts unwritten"
         return res
 

@@ -82,6 +82,73 @@ def test_checker_matches_reference_gpu_checker(robot, kind, seed, ctx, oracle):
     assert np.all(margin[bad] < NEAR)
 
 
+def test_checker_faster_than_reference_gpu_checker(ctx):
+    """Device time of prrtc_validate_configs against pRRTC's own checker
+    kernel (fkcc<Robot>, utils.cuh:326-327, one configuration per thread in
+    128-thread blocks, as pRRTC.cu:441,529 check interpolated points) on the
+    same 2^20 configurations: uniformly random, then collision-free (the
+    random set's free configurations repeated).  L2 is flushed before every
+    launch; median of 5 after one warm-up.  Both kernels see the same inputs
+    already on the device; the table prints with `pytest -s`.  The verdicts
+    are counted against each other (parity proper is the test above) and
+    the library's kernel must be the faster in every case."""
+    import statistics
+
+    import torch
+    from pyoracle import RefGpuChecker
+    from prrtc_gb300 import scenes
+    if not all(RefGpuChecker.available(r) for r in ("panda", "fetch", "baxter")):
+        pytest.skip("reference GPU checker not built (needs a pRRTC checkout at build time)")
+    n = 1 << 20
+    cases = [("panda", "tabletop 0", scenes.tabletop_scene(0)), ("panda", "shelf 1", scenes.shelf_scene(1))]
+    cases += [(r, f"{k} {s}, all types", scene(r, k, s)) for r, k, s in SCENES]
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+
+    def timed(fn):
+        ms = []
+        for _ in range(6):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            ms.append(fn())
+        return statistics.median(ms[1:])
+
+    def ref_ms(run):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        run()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b)
+
+    rows = []
+    for robot, label, env in cases:
+        ref = RefGpuChecker(robot)
+        e = ctx.upload_env(env)
+        sc, off = (np.array(v) for v in scenes.LIMITS[robot])
+        rnd = (np.random.default_rng(7).random((n, len(sc))) * sc + off).astype(np.float32)
+        qr = torch.from_numpy(rnd).cuda()
+        free = ctx.validate_configs(robot, e, qr).cpu().numpy().astype(bool)
+        qf = torch.from_numpy(np.ascontiguousarray(np.resize(rnd[free], (n, len(sc))))).cuda()
+        for kind, q in (("random", qr), ("free", qf)):
+            run, out = ref.prepare(env, q)
+            t_ref = timed(lambda: ref_ms(run))
+            got = []
+
+            def ours():
+                got.append(ctx.validate_configs(robot, e, q))
+                torch.cuda.synchronize()
+                return ctx.last_kernel_ns() / 1e6
+            t_ours = timed(ours)
+            mism = int((got[-1] != out).sum().item())
+            rows.append((robot, label, kind, t_ref, t_ours, mism))
+    print("\nrobot   scene                    configs  pRRTC fkcc ms  library ms  speed-up  mismatches")
+    for robot, label, kind, t_ref, t_ours, mism in rows:
+        print(f"{robot:7s} {label:24s} {kind:7s}  {t_ref:13.3f}  {t_ours:10.3f}  {t_ref / t_ours:7.2f}x  {mism}")
+    for robot, label, kind, t_ref, t_ours, mism in rows:
+        assert mism <= n // 100000, (robot, label, kind, mism)
+        assert t_ours < t_ref, (robot, label, kind, t_ours, t_ref)
+
+
 @pytest.mark.parametrize("case", golden_cases())
 def test_fk_spheres_match_fp64(case, ctx, oracle):
     robot = case.split("_")[0]
