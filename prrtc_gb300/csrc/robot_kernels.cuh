@@ -41,8 +41,8 @@ __device__ __forceinline__ void add_work(unsigned long long *work, unsigned long
 // of 16 hide its dependency waits better (2^20 random configurations: Panda
 // 1.23 vs 1.27 ms on the tabletop scene and 1.81 vs 1.97 ms on the shelf,
 // Baxter 3.70 ms against 4.50 ms unconstrained and 4.53 ms at 122 registers
-// on a shelf scene); a robot file may specialise it (Fetch, 4.5 vs 4.8 ms,
-// keeps its 104 registers).
+// on a shelf scene; Fetch, table form, 5.28 ms against 5.56 ms
+// unconstrained); a robot file may specialise it.
 template <class Gen>
 struct ValidateLaunch {
     static constexpr int kMaxThreads = 128, kMinBlocks = 8;

@@ -37,11 +37,13 @@ INLINE_LEAVES = 6   # leaf blocks up to this size are emitted as straight-line t
 # Baxter's 388 groups as straight-line code overflow the instruction cache
 # (its planner kernel stalled on instruction fetch 33 times per issue).
 TABLE_ROBOTS = ("panda", "fetch", "baxter")
-# Robots that also get the straight-line form, as fkcc_validate: the stand-alone
-# checker on uniformly random configurations, most of which collide at the
-# first groups, runs up to 2x faster without computing every frame first.
-# (Baxter's straight-line form does not fit the instruction cache.)
-INLINE_VALIDATE = ("sphere", "panda", "fetch")
+# Robots that also get the straight-line form, as fkcc_validate: Panda's
+# stand-alone checker runs 6 % faster with it than with the table form (2^20
+# random configurations, tabletop scene: 1.24 vs 1.32 ms).  Fetch's runs 2 %
+# faster in table form at 64 registers (mixed scene: 5.28 vs 5.38 ms) and
+# Baxter's straight-line form does not fit the instruction cache, so both
+# use the table form for single configurations too.
+INLINE_VALIDATE = ("sphere", "panda")
 
 
 def load_model(robot: str) -> dict:
