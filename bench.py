@@ -382,7 +382,11 @@ def ours(args, rank, world):
         "validator": validator,
         "e2e": {"value": e2e_solved / e2e_t, "unit": "queries/s", "h2d_bytes_per_step": int(h2d) // args.steps,
                 "d2h_bytes_per_step": int(d2h) // args.steps, "call_ms": e2e_t * 1e3,
-                "create_ms": res_e2e[0].copy_ns / 1e6 if res_e2e else None},
+                "create_ms": res_e2e[0].copy_ns / 1e6 if res_e2e else None,
+                "launch_ms": max((r.finish_ns for r in res_e2e), default=0) / 1e6,
+                "split": "call_ms = create_ms (packing and upload) + launch_ms (this call's own launch, "
+                         "from its start to the last query's end; its tail varies from run to run like "
+                         "the device-timed launch's) + result copies, unpacking and release"},
         "e2e_python": {"value": e2e_py_solved / e2e_py_t, "unit": "queries/s",
                        "note": "Context.solve_batch: the Python wrapper's marshalling and unpacking included"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
