@@ -191,7 +191,10 @@ prrtc_status prrtc_validate_edges(prrtc_ctx *ctx, prrtc_robot robot, const prrtc
  * call on a device shares it, so calls whose GPU work overlaps (other
  * streams, other threads) race: serialise them.  The first call on a device
  * looks up the array's address with that device current; make it before any
- * stream capture.
+ * stream capture.  The call cannot be captured into a CUDA graph (a replay
+ * would copy whatever the host array holds at that time): while `stream` is
+ * being captured it returns PRRTC_EINVAL without touching the stream, and the
+ * capture stays valid.
  */
 prrtc_status prrtc_validate_configs_noalloc(prrtc_robot robot, const prrtc_env_desc *env, const float *q,
                                             int64_t n, uint8_t *out_free, void *stream);

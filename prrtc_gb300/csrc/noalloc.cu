@@ -19,7 +19,8 @@
 // whose work overlaps on the GPU (different streams, or different host
 // threads) race on it: serialise them.  The first call on a device looks up
 // the array's device address (cudaGetSymbolAddress) with that device current;
-// make that first call before any stream capture.
+// make that first call before any stream capture.  A call made while its
+// stream is being captured returns PRRTC_EINVAL and records nothing.
 #include <cstring>
 #include <mutex>
 
@@ -90,11 +91,21 @@ extern "C" prrtc_status prrtc_validate_configs_noalloc(prrtc_robot robot, const 
                             16ull * env->num_cuboids + 16ull * env->num_z_aligned_cuboids;
     if (floats > (uint64_t)PRRTC_MAX_ENV_FLOATS) return PRRTC_EINVAL;   // larger than the scratch array
     if (n == 0) return PRRTC_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // Not capturable into a graph: the obstacles are copied from the library's
+    // host array at call time, and a replay would copy whatever that array
+    // holds then.  Under stream capture the call refuses before it touches
+    // the stream, so the caller's capture stays valid.
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &capture) != cudaSuccess) {
+        cudaGetLastError();
+        return PRRTC_ECUDA;
+    }
+    if (capture != cudaStreamCaptureStatusNone) return PRRTC_EINVAL;
     void *scratch = nullptr;
     int sms = 0;
     prrtc_status s = scratch_on_current_device(&scratch, &sms);
     if (s) return s;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     unsigned long long *work = reinterpret_cast<unsigned long long *>(static_cast<unsigned char *>(scratch) + kEnvBytes);
     {
         std::lock_guard<std::mutex> g(g_pack_mu);

@@ -99,3 +99,40 @@ def test_noalloc_rejects_environment_beyond_the_fixed_array():
     qd = torch.zeros((4, 7), dtype=torch.float32, device="cuda")
     out = torch.zeros(4, dtype=torch.uint8, device="cuda")
     assert f(api.robot_id("panda"), C.byref(d), qd.data_ptr(), 4, out.data_ptr(), None) == 1   # PRRTC_EINVAL
+
+
+def test_noalloc_refuses_stream_capture():
+    """The call copies its obstacles from a library host array when it runs,
+    so it is not capturable into a CUDA graph.  While the stream is being
+    captured it must return PRRTC_EINVAL and leave the stream alone: the
+    capture ends cleanly, and a replay runs only the work captured around
+    the refused call."""
+    import torch
+    from prrtc_gb300 import api, scenes
+    f = _noalloc()
+    env = scenes.shelf_scene(3)
+    sc, off = (np.array(v) for v in scenes.LIMITS["panda"])
+    q = (np.random.default_rng(9).random((4096, 7)) * sc + off).astype(np.float32)
+    qd = torch.from_numpy(q).cuda()
+    out = torch.full((len(q),), 7, dtype=torch.uint8, device="cuda")
+    d, keep = api._env_desc(env)
+    s = torch.cuda.Stream()
+    # an ordinary call first, on the same stream (the per-device setup)
+    assert f(api.robot_id("panda"), C.byref(d), qd.data_ptr(), len(q), out.data_ptr(), C.c_void_p(s.cuda_stream)) == 0
+    s.synchronize()
+    first = out.clone()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        status = f(api.robot_id("panda"), C.byref(d), qd.data_ptr(), len(q), out.data_ptr(),
+                   C.c_void_p(s.cuda_stream))
+        out.add_(0)   # captured work beside the refused call, so the graph is not empty
+    assert status == 1   # PRRTC_EINVAL
+    out.fill_(7)
+    torch.cuda.synchronize()
+    g.replay()
+    torch.cuda.synchronize()
+    assert (out == 7).all()   # the replay did not write verdicts: nothing of the call was recorded
+    out.copy_(first)
+    assert f(api.robot_id("panda"), C.byref(d), qd.data_ptr(), len(q), out.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy(), first.cpu().numpy())
