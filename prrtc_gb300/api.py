@@ -413,7 +413,13 @@ class Context:
         """The host side of prrtc_solve_batch's arguments: the prrtc_query
         array (pointing at host start, goal and obstacle arrays) and the
         prrtc_result array with its path buffers, built as numpy arrays with
-        the C structs' layouts (no per-query ctypes work)."""
+        the C structs' layouts (no per-query ctypes work).  The path buffers
+        (`paths`, path_capacity rows per query) are fresh memory: the first
+        call that writes them also pays the operating system's zeroing of
+        their pages (each query's buffer starts a new 64 KB page on a
+        system with 64 KB pages: ~40 ms for 20 480 queries).  A caller
+        that cares about the call's latency reuses the PreparedBatch or
+        writes `paths` once beforehand."""
         rid = robot_id(robot)
         D, n = dof(rid), len(queries)
         trip = [q if isinstance(q, tuple) else (q.env, q.start, q.goal) for q in queries]
