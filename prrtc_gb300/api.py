@@ -416,8 +416,9 @@ class Context:
         the C structs' layouts (no per-query ctypes work).  The path buffers
         (`paths`, path_capacity rows per query) are fresh memory: the first
         call that writes them also pays the operating system's zeroing of
-        their pages (each query's buffer starts a new 64 KB page on a
-        system with 64 KB pages: ~40 ms for 20 480 queries).  A caller
+        their pages (at 2048 rows of 7 floats per query, nearly every
+        query's path lands on a page of its own: ~40 ms for 20 480 queries
+        with 64 KB pages).  A caller
         that cares about the call's latency reuses the PreparedBatch or
         writes `paths` once beforehand."""
         rid = robot_id(robot)
