@@ -142,15 +142,31 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
     const int D = ops->dof;
     int cap = settings->max_nodes_per_tree > 0 ? settings->max_nodes_per_tree : std::min(S.max_samples, 65536);
     cap = std::max(4, (std::min(cap, S.max_samples) + 3) & ~3);
-    // pack queries
-    std::vector<float> cfg;
-    std::vector<float4> envs;
-    std::vector<BatchQueryDesc> descs(n);
-    std::vector<int> env_rec_off(n, -1);
+    // pack queries: sizes first (every query checked), so that the packed
+    // configurations and obstacle records are allocated once and written in
+    // place, with no per-query temporaries
+    size_t cfg_floats = 0, env_records = 0;
     for (int i = 0; i < n; i++) {
         const prrtc_query &q = queries[i];
         if (!q.start || !q.goals || q.num_goals < 1 || q.num_goals >= cap || (!q.env && !q.env_desc))
             return c->fail(PRRTC_EINVAL, "batch_create: bad query %d", i);
+        cfg_floats += (size_t)(1 + q.num_goals) * D;
+        if (!q.env) {
+            const prrtc_env_desc &e = *q.env_desc;
+            const uint64_t recs = (uint64_t)e.num_spheres + 2ull * e.num_capsules + 2ull * e.num_z_aligned_capsules +
+                                  4ull * e.num_cuboids + 4ull * e.num_z_aligned_cuboids;
+            if (recs * 4 > (uint64_t)PRRTC_MAX_ENV_FLOATS) return c->fail(PRRTC_EINVAL, "batch_create: env %d too large", i);
+            env_records += recs;
+        }
+    }
+    std::vector<float> cfg;
+    std::vector<float4> envs;
+    cfg.reserve(cfg_floats);
+    envs.reserve(env_records);
+    std::vector<BatchQueryDesc> descs(n);
+    std::vector<int> env_rec_off(n, -1);
+    for (int i = 0; i < n; i++) {
+        const prrtc_query &q = queries[i];
         descs[i].cfg_off = (int)cfg.size();
         descs[i].num_goals = q.num_goals;
         cfg.insert(cfg.end(), q.start, q.start + D);
@@ -160,15 +176,11 @@ extern "C" prrtc_status prrtc_batch_create(prrtc_ctx *ctx, prrtc_robot robot, co
             descs[i].env = e->dev;
             descs[i].env_n = e->counts;
         } else {
-            std::vector<float4> rec;
-            pack_env(*q.env_desc, rec);
-            EnvCounts nc{(int)q.env_desc->num_spheres, (int)q.env_desc->num_capsules,
-                         (int)q.env_desc->num_z_aligned_capsules, (int)q.env_desc->num_cuboids,
-                         (int)q.env_desc->num_z_aligned_cuboids};
-            if ((int64_t)nc.records() * 4 > PRRTC_MAX_ENV_FLOATS) return c->fail(PRRTC_EINVAL, "batch_create: env %d too large", i);
+            const prrtc_env_desc &e = *q.env_desc;
             env_rec_off[i] = (int)envs.size();
-            descs[i].env_n = nc;
-            envs.insert(envs.end(), rec.begin(), rec.end());
+            descs[i].env_n = EnvCounts{(int)e.num_spheres, (int)e.num_capsules, (int)e.num_z_aligned_capsules,
+                                       (int)e.num_cuboids, (int)e.num_z_aligned_cuboids};
+            pack_records(e, [&](float4 r) { envs.push_back(r); });
         }
     }
     prrtc_batch *b = new prrtc_batch();
