@@ -11,6 +11,21 @@ def test_generated_files_are_current():
     assert codegen.check_up_to_date() == []
 
 
+def test_single_configuration_checker_forms():
+    """The stand-alone checker's form per robot, as measured on the GB300:
+    Panda's fkcc_validate is its own straight-line code; Fetch's and
+    Baxter's delegate to the table-form walk (fkcc); the sphere robot has
+    no table form at all, so both of its entry points are straight-line."""
+    from prrtc_gb300.robots import codegen
+    head = "bool fkcc_validate(const float *__restrict__ q, Ctx &ctx)\n{\n"
+    for robot, delegates, table in (("sphere", True, False), ("panda", False, True), ("fetch", True, True),
+                                    ("baxter", True, True)):
+        text = (codegen.CSRC / f"{robot}_fkcc.cuh").read_text()
+        body = text[text.index(head) + len(head):]
+        assert body.startswith("    return fkcc(q, ctx);\n}") == delegates, robot
+        assert ("run_schedule(" in text) == table, robot
+
+
 @pytest.mark.parametrize("case", golden_cases())
 def test_model_fk_matches_reference_fp64(case, oracle):
     """Oracle float64 FK of the fitted model vs the reference's generated FK
